@@ -1,0 +1,437 @@
+"""Throughput benchmark of the emsim multislice hot path on GB300.
+
+Workload (one step): a batch of protein-like blobs, each 50,000 C/N/O/S atoms
+(fractions 0.63/0.17/0.19/0.01, seeded) uniform in a 40 A sphere, imaged at roi 256,
+resolution 2 A (pixel 1 A), slice thickness 2 A (40 slices), 200 keV, Cs 1.3 mm,
+defocus 700 A, aperture 10 mrad, plain FP32: atom binning -> projected-potential
+slices -> multislice -> lens -> |psi|^2.  Inputs are resident in HBM for ``value``;
+``e2e`` runs the same images through the public ``Pipe.run`` API from host atoms to a
+host image.  L2 is flushed (256 MiB write) before every timed step; each step is timed
+with CUDA events on the launching stream.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl reference]
+
+Multi-GPU (torchrun): every rank images its own blobs (weak scaling, no collective on
+the data path); rank 0 prints the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = dict(n_atoms=50_000, radius=40.0, roi=256, resolution=2.0, slice_thickness=2.0, kev=200.0,
+                cs_mm=1.3, defocus=700.0, aperture=10e-3, dose=20.0)
+METRIC = "images/s (50k-atom blob, 256^2, 40 slices, plain FP32)"
+
+
+def blob(seed: int):
+    from oracle.multislice import protein_blob  # seeded synthetic input generator
+    return protein_blob(WORKLOAD["n_atoms"], WORKLOAD["radius"], seed)
+
+
+def rank_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------------
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.rows = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------
+class DeviceBatch:
+    """Device-resident inputs and buffers for B blobs; run() queues one full step."""
+
+    def __init__(self, seeds, torch, backend, atoms, pot):
+        W = WORKLOAD
+        self.torch = torch
+        self.backend = backend
+        dev = torch.device("cuda", torch.cuda.current_device())
+        pix = 0.5 * W["resolution"]
+        self.pix = pix
+        self.items = []
+        ns_all = set()
+        for s in seeds:
+            el, xyz = blob(s)
+            mol = atoms.centralize(atoms.AtomList(el, xyz))
+            mol, uz, cnt = atoms.sort_elements_and_count(mol)
+            ns, n1, n2 = pot.finalize_slice_size(tuple(mol.space), (pix, pix), W["slice_thickness"], W["roi"], None)
+            ns_all.add(ns)
+            self.items.append((torch.from_numpy(mol.coordinates).to(dev), list(uz),
+                               torch.from_numpy(cnt.astype(np.int32)).to(dev), ns))
+        self.ns = max(ns_all)
+        self.n = W["roi"]
+        self.B = len(seeds)
+        # one builder (plan) per distinct (elements, n_slices); slice stacks padded to ns
+        self.builders = {}
+        for c, uz, cnt, ns in self.items:
+            key = (tuple(uz), ns)
+            if key not in self.builders:
+                self.builders[key] = backend.MultiSlicesBuilder(uz, ns, self.n, self.n, W["slice_thickness"], pix, pix)
+        self.hist = {k: torch.empty((len(k[0]), k[1], self.n, self.n), dtype=torch.float32, device=dev)
+                     for k in self.builders}
+        self.slices = torch.zeros((self.B, self.ns, self.n, self.n), dtype=torch.float32, device=dev)
+        self.work = torch.empty((self.B, self.n, self.n), dtype=torch.complex64, device=dev)
+        self.img = torch.empty((self.B, self.n, self.n), dtype=torch.float32, device=dev)
+        self.ws = {k: torch.empty(max(256, int(backend._native.load().emsim_gb300_make_slices_workspace_size(
+            b._plan.handle))), dtype=torch.uint8, device=dev) for k, b in self.builders.items()}
+        self.wp = backend.WavePropagator(self.n, self.n, pix, pix, W["kev"])
+        self.df = np.full(self.B, W["defocus"], dtype=np.float64)
+        if len(ns_all) != 1:
+            raise RuntimeError(f"blobs of one batch need equal slice counts, got {sorted(ns_all)}")
+
+    def launches_per_step(self) -> int:
+        per_image = 1 + 3  # binning kernel + three slice-build passes (memset is a driver op)
+        lens = math.ceil(self.B / 64)
+        return self.B * per_image + 2 * self.ns + lens + 1
+
+    def run(self):
+        import ctypes
+        nat = self.backend._native
+        st = ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+        P = self.backend._ptr
+        for b, (c, uz, cnt, ns) in enumerate(self.items):
+            key = (tuple(uz), ns)
+            plan = self.builders[key]._plan.handle
+            h = self.hist[key]
+            nat.call("emsim_gb300_bin_atoms_multi_slices", plan, P(c), int(c.shape[0]), P(cnt), P(h), st)
+            ws = self.ws[key]
+            nat.call("emsim_gb300_make_slices", plan, P(h), P(self.slices[b]), P(ws), ws.numel(), st)
+        W = WORKLOAD
+        nat.call("emsim_gb300_multislice_image", self.wp._plan.handle, P(self.slices), self.ns,
+                 self.ns * self.n * self.n, W["slice_thickness"], W["dose"], W["cs_mm"],
+                 self.df.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self.B, W["aperture"], P(self.img),
+                 P(self.work), None, self.B, st)
+
+
+def slice_step_roofline(torch, backend, n: int, n_img: int, n_slices: int, peak_gbs: float, reps: int = 5):
+    """Average duration of one slice step (fused row pass + column pass) on a batch of
+    n_img waves of n x n, from CUDA events around multislice_propagate calls."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    wp = backend.WavePropagator(n, n, 0.5, 0.5, 200.0)
+    w = torch.ones((n_img, n, n), dtype=torch.complex64, device=dev)
+    sl = torch.rand((n_img, n_slices, n, n), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(2):
+        wp.multislice_propagate(w, sl, 2.0)
+    ts = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        wp.multislice_propagate(w, sl, 2.0)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = float(np.median(ts))
+    # n_slices steps + one final row pass (the inverse rows of the exit wave)
+    per_step = t / (n_slices + 0.5)
+    algo = 20.0 * n * n * n_img  # bytes per slice step: psi read 8 + psi write 8 + V read 4
+    return {"n": n, "images": n_img, "slices": n_slices, "step_s": per_step,
+            "slice_steps_per_s": n_img / per_step, "achieved_gbs": algo / per_step / 1e9,
+            "frac": algo / per_step / 1e9 / peak_gbs}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = rank_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    from emsim_gb300 import atoms, backend, pipe, pot, tem
+    from emsim_gb300 import build as b
+    b.build()
+
+    B = args.batch
+    seeds = [1000 * rank + i for i in range(B)]
+    db = DeviceBatch(seeds, torch, backend, atoms, pot)
+    dev = torch.device("cuda", local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # warm-up (plans, propagator tables, lazy module loading)
+    for _ in range(args.warmup):
+        db.run()
+    torch.cuda.synchronize()
+    graph = None
+    if not args.no_graph:
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=s):
+                db.run()
+        torch.cuda.current_stream().wait_stream(s)
+        graph.replay()
+        torch.cuda.synchronize()
+
+    def step():
+        if graph is not None:
+            graph.replay()
+        else:
+            db.run()
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+    torch.cuda.synchronize()
+    t_total = float(sum(times))
+    if world > 1:
+        tt = torch.tensor([t_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+        dist.barrier()
+    value = B * world * args.steps / t_total
+
+    # ---- end to end through the public API (host atoms -> host image) ----------
+    W = WORKLOAD
+    t_ = tem.TEM(electron_dose=W["dose"], beam_energy_kev=W["kev"], cs_mm=W["cs_mm"], defocus=W["defocus"],
+                 aperture=W["aperture"])
+    p = pipe.Pipe(t_, resolution=W["resolution"], slice_thickness=W["slice_thickness"], roi=W["roi"],
+                  add_water=False)
+    mols = []
+    h2d = 0
+    for s in seeds:
+        el, xyz = blob(s)
+        mols.append(atoms.AtomList(el, xyz))
+        h2d += xyz.nbytes + 4 * 4  # coordinates + per-element counts
+    for m in mols[:2]:
+        p.run(m).get()
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        imgs = p.run_batch(mols)
+        host = [im.get() for im in imgs]
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": len(mols) * e2e_steps / t_e2e, "unit": "images/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": int(sum(x.nbytes for x in host)), "api": "emsim_gb300.pipe.Pipe.run_batch",
+           "timing": "wall clock, host front-end (sort by element, sizing) included"}
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # ---- accuracy of the benched image vs the FP64 oracle (outside timing) ----------
+    from oracle import multislice as om
+    el, xyz = blob(seeds[0])
+    ref64 = om.pipe_run(el, xyz, resolution=W["resolution"], slice_thickness=W["slice_thickness"], roi=W["roi"],
+                        beam_energy_kev=W["kev"], dose=W["dose"], cs_mm=W["cs_mm"], defocus=W["defocus"],
+                        aperture=W["aperture"], semantics="fftw", dtype=np.float64)
+    img0 = db.img[0].cpu().numpy()
+    acc = {"rel_l2_image_vs_fp64": om.rel_l2(img0, ref64),
+           "rel_l2_contrast_vs_fp64": om.rel_l2(img0 - img0.mean(), ref64 - ref64.mean())}
+
+    # ---- roofline of the dominant kernel pair (slice step) ----------------------
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    rl = {}
+    for n, n_img, ns in [(256, B, db.ns), (512, 32, 16), (2048, 2, 16)]:
+        rl[n] = slice_step_roofline(torch, backend, n, n_img, ns, peak)
+    traffic = read_traffic()
+    main = rl[256]
+    roofline = {"bound": "hbm", "kernel": "slice step = row_pass_kernel + col_pass_kernel (256^2, batch %d)" % B,
+                "achieved": round(main["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
+                "frac": round(main["frac"], 4), "traffic": traffic.get("slice_step_256"),
+                "peak_source": peak_src, "algorithmic_bytes_per_launch": 20 * 256 * 256 * B}
+
+    # ---- CPU baseline: the oracle's restatement of the reference numpy path ------
+    cpu = cpu_baseline(budget_s=args.cpu_seconds)
+
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "images/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * t_total / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (complex64 waves)", "data": "synthetic (seeded blobs)",
+        "config": {"workload": "blob 50k C/N/O/S atoms r=40A, roi 256, pixel 1A, dz 2A, %d slices, 200 keV, "
+                               "Cs 1.3 mm, df 700 A, aperture 10 mrad" % db.ns,
+                   "images_per_step_per_gpu": B, "l2": "flushed (256 MiB write) before every timed step",
+                   "cuda_graph": graph is not None, "parallelism": f"image-parallel x{world}"},
+        "slice_steps_per_s": round(value * db.ns, 1),
+        "slice_step_throughput": {str(k): {"slice_steps_per_s": round(v["slice_steps_per_s"], 1),
+                                           "hbm_frac": round(v["frac"], 4), "images": v["images"]}
+                                  for k, v in rl.items()},
+        "accuracy": acc,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": db.launches_per_step() * args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def read_traffic():
+    """DRAM bytes per launch from the committed ncu summary (profiles/dram_traffic.txt)."""
+    f = ROOT / "profiles" / "dram_traffic.txt"
+    out = {}
+    if f.exists():
+        for line in f.read_text().splitlines():
+            if line.startswith("#") or "=" not in line:
+                continue
+            k, v = line.split("=", 1)
+            try:
+                out[k.strip()] = float(v.split()[0])
+            except ValueError:
+                pass
+    return out
+
+
+# ---------------------------------------------------------------------------------
+# CPU reference: the oracle's bit-exact restatement of the reference numpy backend
+# ---------------------------------------------------------------------------------
+def _cpu_one(seed: int) -> float:
+    os.environ.setdefault("EMSIM_ORACLE_WORKERS", "1")
+    from oracle import multislice as om
+    W = WORKLOAD
+    el, xyz = blob(seed)
+    t0 = time.perf_counter()
+    om.pipe_run(el, xyz, resolution=W["resolution"], slice_thickness=W["slice_thickness"], roi=W["roi"],
+                beam_energy_kev=W["kev"], dose=W["dose"], cs_mm=W["cs_mm"], defocus=W["defocus"],
+                aperture=W["aperture"], semantics="numpy")
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(budget_s: float = 15.0, processes: int = 1):
+    """Images/s of the reference numpy algorithm on host cores (bounded sample)."""
+    import multiprocessing as mp
+    t0 = time.perf_counter()
+    n = 0
+    if processes <= 1:
+        while time.perf_counter() - t0 < budget_s or n == 0:
+            _cpu_one(n)
+            n += 1
+        dt = time.perf_counter() - t0
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(processes) as pool:
+            pool.map(_cpu_one, range(processes))  # import + warm
+            t0 = time.perf_counter()
+            rounds = 0
+            while time.perf_counter() - t0 < budget_s or rounds == 0:
+                pool.map(_cpu_one, range(processes))
+                rounds += 1
+            dt = time.perf_counter() - t0
+            n = rounds * processes
+    return {"value": round(n / dt, 4), "unit": "images/s", "cores": processes, "kind": "port",
+            "sample": f"{n} image(s) of the bench workload through the reference numpy algorithm "
+                      f"(oracle 'numpy' semantics, bit-exact with emsim's numpy backend, complex128, "
+                      f"numpy FFT) in {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = rank_env()
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    budget = max(5.0, args.cpu_seconds)
+    vals = []
+    for _ in range(args.warmup):
+        _cpu_one(0)
+    for k in range(args.steps):
+        c = cpu_baseline(budget_s=budget / max(1, args.steps), processes=procs)
+        vals.append(c["value"])
+    v = float(np.median(vals))
+    out = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "images/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64 (numpy complex128)", "data": "synthetic (seeded blobs)",
+           "config": {"workload": "blob 50k C/N/O/S atoms r=40A, roi 256, pixel 1A, dz 2A, 40 slices, 200 keV",
+                      "parallelism": f"{procs} host processes"},
+           "cpu_baseline": {"value": round(v, 4), "unit": "images/s", "cores": procs, "kind": "port",
+                            "sample": "reference numpy algorithm (bit-exact oracle restatement; the reference "
+                                      "tree is not present on the GPU host), one image per process per round"},
+           "e2e": {"value": round(v, 4), "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-graph", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,95 @@
+"""ctypes binding of the engine's C ABI (``include/emsim_gb300.h``).
+
+The shared library is built in-tree by ``emsim_gb300.build``.  There is no fallback:
+when the library is missing or fails to load, every entry point raises
+:class:`NativeUnavailable`.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libemsim_gb300.so"
+
+_c_int, _c_ll, _c_dbl, _c_uint, _c_vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_uint, ctypes.c_void_p
+_c_size = ctypes.c_size_t
+_pp = ctypes.POINTER(ctypes.c_void_p)
+
+# name -> (restype, argtypes); mirrors include/emsim_gb300.h one to one
+SIGNATURES = {
+    "emsim_gb300_abi_version": (_c_int, []),
+    "emsim_gb300_last_error": (ctypes.c_char_p, []),
+    "emsim_gb300_wave_plan_create": (_c_int, [_c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _pp]),
+    "emsim_gb300_wave_plan_destroy": (_c_int, [_c_vp]),
+    "emsim_gb300_init_wave": (_c_int, [_c_vp, _c_dbl, _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_slice_transmit": (_c_int, [_c_vp, _c_vp, _c_vp, _c_ll, _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_space_propagate": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_singleslice_propagate": (_c_int, [_c_vp, _c_vp, _c_vp, _c_ll, _c_dbl, _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_multislice_propagate": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_ll, _c_dbl, _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_lens_propagate": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_dbl, _c_dbl, _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_intensity": (_c_int, [_c_vp, _c_vp, _c_ll, _c_vp]),
+    "emsim_gb300_multislice_image": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_dbl, _c_dbl, _c_dbl,
+                                              ctypes.POINTER(ctypes.c_double), _c_int, _c_dbl, _c_vp, _c_vp,
+                                              _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_slice_plan_create": (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl,
+                                               _c_int, _pp]),
+    "emsim_gb300_slice_plan_destroy": (_c_int, [_c_vp]),
+    "emsim_gb300_bin_atoms_one_slice": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_vp, _c_vp]),
+    "emsim_gb300_bin_atoms_multi_slices": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_vp, _c_vp]),
+    "emsim_gb300_make_slices_workspace_size": (_c_size, [_c_vp]),
+    "emsim_gb300_make_slices": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_size, _c_vp]),
+}
+
+ERROR_NAMES = {1: "invalid argument", 2: "CUDA error", 3: "unsupported", 4: "wrong device"}
+
+
+class NativeUnavailable(ImportError):
+    """The compiled engine library is missing or could not be loaded."""
+
+
+class NativeError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn}: {ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: Path | str | None = None):
+    """Load (once) and return the ctypes library with every signature declared."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise NativeUnavailable(
+                f"emsim_gb300 native library not found at {p}; build it with `python -m emsim_gb300.build`")
+        try:
+            lib = ctypes.CDLL(str(p))
+        except OSError as e:  # pragma: no cover - depends on the host
+            raise NativeUnavailable(f"cannot load {p}: {e}") from e
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def call(name: str, *args) -> None:
+    """Call a status-returning entry point and raise NativeError on failure."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != 0:
+        raise NativeError(name, st, lib.emsim_gb300_last_error().decode(errors="replace"))
+
+
+def last_error() -> str:
+    return load().emsim_gb300_last_error().decode(errors="replace")

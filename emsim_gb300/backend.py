@@ -1,0 +1,334 @@
+"""emsim backend classes on the GB300 engine - the plugin boundary.
+
+emsim resolves three classes from the current backend at every call
+(emsim/config.py:31-41): ``OneSliceBuilder``, ``MultiSlicesBuilder`` and
+``WavePropagator``.  This module provides them with the reference's constructor
+arguments, method names, argument meaning and return shapes
+(backend/slice_builder_base.py:8-163, backend/wave_propagator_base.py:10-44,
+backend/*_cuda.py), computing through the C ABI of ``include/emsim_gb300.h``.
+
+Arrays: inputs may be numpy arrays, torch tensors (any device) or objects exposing
+``__cuda_array_interface__`` (cupy); outputs are torch CUDA tensors of class
+:class:`DeviceArray`, which add the ``.get()`` host copy that emsim's simulator calls
+on GPU results (simulator.py:51-53).  Work is queued on the current torch CUDA stream.
+
+Extensions beyond the reference signatures (all optional): a leading batch axis on
+waves and slices, ``Pipe``-style fused image formation in ``WavePropagator.image``.
+"""
+from __future__ import annotations
+
+import ctypes
+import logging
+import threading
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _native, elem, physics
+
+logger = logging.getLogger(__name__)
+
+
+class DeviceArray(torch.Tensor):
+    """A torch CUDA tensor with ``get()`` returning a numpy copy (cupy's spelling)."""
+
+    def get(self) -> np.ndarray:
+        return self.detach().cpu().numpy()
+
+
+def _wrap(t: torch.Tensor) -> DeviceArray:
+    return t.as_subclass(DeviceArray)
+
+
+def _device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("emsim_gb300 needs a CUDA device")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _stream() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
+
+
+def as_device(x, dtype: torch.dtype) -> torch.Tensor:
+    """Contiguous tensor of ``dtype`` on the current CUDA device (copy only if needed)."""
+    dev = _device()
+    if isinstance(x, torch.Tensor):
+        t = x
+    elif hasattr(x, "__cuda_array_interface__"):
+        t = torch.as_tensor(x, device=dev)
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(x)))
+    if t.dtype != dtype:
+        t = t.to(dtype)
+    if t.device != dev:
+        t = t.to(dev, non_blocking=False)
+    return t.contiguous()
+
+
+# ---------------------------------------------------------------------------------
+# native plans (cached: the reference builds a new propagator and FFT plan per image,
+# pipe.py:31-34; plans here depend only on geometry and are reused)
+# ---------------------------------------------------------------------------------
+class _Plan:
+    def __init__(self, handle: ctypes.c_void_p, destroy: str):
+        self.handle = handle
+        self._destroy = destroy
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            if self.handle and _native._lib is not None:
+                getattr(_native._lib, self._destroy)(self.handle)
+        except Exception:
+            pass
+
+
+_plan_lock = threading.Lock()
+_wave_plans: Dict[tuple, _Plan] = {}
+_slice_plans: Dict[tuple, _Plan] = {}
+
+
+def wave_plan(n1: int, n2: int, d1: float, d2: float, wave_length: float, gamma: float) -> _Plan:
+    key = (torch.cuda.current_device(), n1, n2, float(d1), float(d2), float(wave_length), float(gamma))
+    with _plan_lock:
+        p = _wave_plans.get(key)
+        if p is None:
+            h = ctypes.c_void_p()
+            _native.call("emsim_gb300_wave_plan_create", n1, n2, float(d1), float(d2), float(wave_length),
+                         float(gamma), ctypes.byref(h))
+            p = _wave_plans[key] = _Plan(h, "emsim_gb300_wave_plan_destroy")
+        return p
+
+
+def slice_plan(unique_elements: Sequence[int], n_slices: int, n1: int, n2: int, dz: float, d1: float, d2: float,
+               bandlimit: bool = True) -> Tuple[_Plan, np.ndarray]:
+    zs = tuple(sorted(int(z) for z in unique_elements))
+    key = (torch.cuda.current_device(), zs, n_slices, n1, n2, float(dz), float(d1), float(d2), bool(bandlimit))
+    sf = elem.scattering_factors_half(zs, n1, n2, d1, d2)
+    with _plan_lock:
+        p = _slice_plans.get(key)
+        if p is None:
+            h = ctypes.c_void_p()
+            _native.call("emsim_gb300_slice_plan_create", sf.ctypes.data_as(ctypes.c_void_p), len(zs), n_slices, n1,
+                         n2, float(dz), float(d1), float(d2), 1 if bandlimit else 0, ctypes.byref(h))
+            p = _slice_plans[key] = _Plan(h, "emsim_gb300_slice_plan_destroy")
+        return p, sf
+
+
+# ---------------------------------------------------------------------------------
+# slice builders
+# ---------------------------------------------------------------------------------
+def _bin(plan: _Plan, fn: str, coords, counts, out_shape) -> DeviceArray:
+    dev = _device()
+    c = as_device(coords, torch.float32).reshape(-1, 3)
+    cnt = as_device(np.asarray(counts, dtype=np.int64).astype(np.uint32).view(np.int32), torch.int32) \
+        if not isinstance(counts, torch.Tensor) else as_device(counts, torch.int32)
+    if cnt.dim() != 1 or cnt.shape[0] != out_shape[0]:
+        raise ValueError(f"unique_elements_count must have {out_shape[0]} entries, got {tuple(cnt.shape)}")
+    out = torch.empty(out_shape, dtype=torch.float32, device=dev)
+    _native.call(fn, plan.handle, _ptr(c), int(c.shape[0]), _ptr(cnt), _ptr(out), _stream())
+    return _wrap(out)
+
+
+def _make(plan: _Plan, hist, n_slices: int, n1: int, n2: int) -> torch.Tensor:
+    dev = _device()
+    h = as_device(hist, torch.float32)
+    out = torch.empty((n_slices, n1, n2), dtype=torch.float32, device=dev)
+    nbytes = int(_native.load().emsim_gb300_make_slices_workspace_size(plan.handle))
+    work = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+    _native.call("emsim_gb300_make_slices", plan.handle, _ptr(h), _ptr(out), _ptr(work), nbytes, _stream())
+    return out
+
+
+class OneSliceBuilder:
+    """One projected-potential slice (slice_builder_base.py:8-73, slice_builder_cuda.py:24-44)."""
+
+    def __init__(self, unique_elements: List[int], n1: int, n2: int, d1: float, d2: float):
+        self.n1, self.n2 = n1, n2
+        self.d1, self.d2 = d1, d2
+        self.unique_elements = unique_elements
+        self._plan, self.scattering_factors = slice_plan(unique_elements, 1, n1, n2, 1.0, d1, d2, True)
+
+    def bin_atoms_one_slice(self, atom_coordinates_sorted_by_elems, unique_elements_count):
+        """(nE, n1, n2) float32 histogram of columns (x, y) = 1, 2."""
+        return _bin(self._plan, "emsim_gb300_bin_atoms_one_slice", atom_coordinates_sorted_by_elems,
+                    unique_elements_count, (len(self.unique_elements), self.n1, self.n2))
+
+    def make_one_slice(self, atom_histograms_one_slice, symmetric_bandlimit: bool = True):
+        """(n1, n2) float32 band-limited projected potential clipped at 1e-13."""
+        plan = self._plan if symmetric_bandlimit else slice_plan(
+            self.unique_elements, 1, self.n1, self.n2, 1.0, self.d1, self.d2, False)[0]
+        return _wrap(_make(plan, atom_histograms_one_slice, 1, self.n1, self.n2)[0])
+
+
+class MultiSlicesBuilder:
+    """Stack of slices (slice_builder_base.py:76-163, slice_builder_cuda.py:47-85)."""
+
+    def __init__(self, unique_elements: List[int], n_slices: int, n1: int, n2: int, dz: float, d1: float,
+                 d2: float):
+        self.n_slice = n_slices
+        self.n1, self.n2 = n1, n2
+        self.dz = dz
+        self.d1, self.d2 = d1, d2
+        self.unique_elements = unique_elements
+        self._plan, self.scattering_factors = slice_plan(unique_elements, n_slices, n1, n2, dz, d1, d2, True)
+
+    def bin_atoms_multi_slices(self, atom_coordinates_sorted_by_elems, unique_elements_count):
+        """(nE, n_slices, n1, n2) float32 histogram of columns (z, x, y)."""
+        return _bin(self._plan, "emsim_gb300_bin_atoms_multi_slices", atom_coordinates_sorted_by_elems,
+                    unique_elements_count, (len(self.unique_elements), self.n_slice, self.n1, self.n2))
+
+    def add_water(self, atom_histograms, generator: Optional[torch.Generator] = None):
+        """Voxel water (slice_builder_base.py:134-147): in voxels empty for every element,
+        add Poisson(0.031 d1 d2 dz) oxygens and Poisson(2x that) hydrogens.  Z = 1 and 8
+        must be among the unique elements."""
+        h = as_device(atom_histograms, torch.float32)
+        vacs = (h == 0).all(dim=0)
+        lam = physics.water_num_dens * self.d1 * self.d2 * self.dz
+        shape = (self.n_slice, self.n1, self.n2)
+        rate = torch.full(shape, lam, dtype=torch.float32, device=h.device)
+        oxy = torch.where(vacs, torch.poisson(rate, generator=generator), torch.zeros_like(rate))
+        hyd = torch.where(vacs, torch.poisson(rate * 2, generator=generator), torch.zeros_like(rate))
+        zs = list(self.unique_elements)
+        h[zs.index(1)] += hyd
+        h[zs.index(8)] += oxy
+        return _wrap(h)
+
+    def make_multi_slices(self, atom_histograms, symmetric_bandlimit: bool = True):
+        """(n_slices, n1, n2) float32 band-limited slices clipped at 1e-13."""
+        plan = self._plan if symmetric_bandlimit else slice_plan(
+            self.unique_elements, self.n_slice, self.n1, self.n2, self.dz, self.d1, self.d2, False)[0]
+        return _wrap(_make(plan, atom_histograms, self.n_slice, self.n1, self.n2))
+
+
+# ---------------------------------------------------------------------------------
+# wave propagator
+# ---------------------------------------------------------------------------------
+class WavePropagator:
+    """Raw wave propagator (wave_propagator_base.py:10-44, wave_propagator_cuda.py:21-60).
+
+    All methods are out-of-place and return complex64 (n1, n2) (or (B, n1, n2) for a
+    batch of B waves) DeviceArrays.  FFT semantics follow the reference's native
+    backends: true fftfreq grid, 2/3 band-limit in every propagation, aperture
+    f^2 <= (alpha/lambda)^2.
+    """
+
+    def __init__(self, n1: int, n2: int, d1: float, d2: float, beam_energy_kev: float):
+        self.wave_shape = (n1, n2)
+        self.d1, self.d2 = d1, d2
+        self.wave_length = physics.electron_wave_length_angstrom(beam_energy_kev)
+        self.relativity_gamma = physics.electron_relativity_gamma(beam_energy_kev)
+        self._plan = wave_plan(n1, n2, d1, d2, self.wave_length, self.relativity_gamma)
+
+    # -- helpers ----------------------------------------------------------------
+    def _wave(self, wave) -> Tuple[torch.Tensor, int]:
+        w = as_device(wave, torch.complex64)
+        n1, n2 = self.wave_shape
+        if w.dim() == 2 and tuple(w.shape) == (n1, n2):
+            return w, 1
+        if w.dim() == 3 and tuple(w.shape[1:]) == (n1, n2):
+            return w, int(w.shape[0])
+        raise ValueError(f"wave must be ({n1}, {n2}) or (B, {n1}, {n2}), got {tuple(w.shape)}")
+
+    def _slice(self, aslice, nb: int) -> Tuple[torch.Tensor, int]:
+        s = as_device(aslice, torch.float32)
+        n1, n2 = self.wave_shape
+        if tuple(s.shape) == (n1, n2):
+            return s, 0
+        if s.dim() == 3 and tuple(s.shape) == (nb, n1, n2):
+            return s, n1 * n2
+        raise ValueError(f"slice must be ({n1}, {n2}) or ({nb}, {n1}, {n2}), got {tuple(s.shape)}")
+
+    def _stack(self, slices, nb: int) -> Tuple[torch.Tensor, int, int]:
+        s = as_device(slices, torch.float32)
+        n1, n2 = self.wave_shape
+        if s.dim() == 3 and tuple(s.shape[1:]) == (n1, n2):
+            return s, int(s.shape[0]), 0
+        if s.dim() == 4 and s.shape[0] == nb and tuple(s.shape[2:]) == (n1, n2):
+            return s, int(s.shape[1]), int(s.shape[1]) * n1 * n2
+        raise ValueError(f"slices must be (n_slices, {n1}, {n2}) or ({nb}, n_slices, {n1}, {n2})")
+
+    # -- the reference API ------------------------------------------------------
+    def init_wave(self, electron_dose: float):
+        out = torch.empty(self.wave_shape, dtype=torch.complex64, device=_device())
+        _native.call("emsim_gb300_init_wave", self._plan.handle, float(electron_dose), _ptr(out), 1, _stream())
+        return _wrap(out)
+
+    def slice_transmit(self, wave, aslice):
+        w, nb = self._wave(wave)
+        s, sstride = self._slice(aslice, nb)
+        out = torch.empty_like(w)
+        _native.call("emsim_gb300_slice_transmit", self._plan.handle, _ptr(w), _ptr(s), sstride, _ptr(out), nb,
+                     _stream())
+        return _wrap(out)
+
+    def space_propagate(self, wave, dz: float):
+        w, nb = self._wave(wave)
+        out = torch.empty_like(w)
+        _native.call("emsim_gb300_space_propagate", self._plan.handle, _ptr(w), float(dz), _ptr(out), nb, _stream())
+        return _wrap(out)
+
+    def singleslice_propagate(self, wave, aslice, dz: float):
+        w, nb = self._wave(wave)
+        s, sstride = self._slice(aslice, nb)
+        out = torch.empty_like(w)
+        _native.call("emsim_gb300_singleslice_propagate", self._plan.handle, _ptr(w), _ptr(s), sstride, float(dz),
+                     _ptr(out), nb, _stream())
+        return _wrap(out)
+
+    def multislice_propagate(self, wave, slices, dz: float):
+        w, nb = self._wave(wave)
+        s, ns, sstride = self._stack(slices, nb)
+        out = torch.empty_like(w)
+        _native.call("emsim_gb300_multislice_propagate", self._plan.handle, _ptr(w), _ptr(s), ns, sstride, float(dz),
+                     _ptr(out), nb, _stream())
+        return _wrap(out)
+
+    def lens_propagate(self, wave, cs_mm: float, defocus: float, aperture: float):
+        w, nb = self._wave(wave)
+        out = torch.empty_like(w)
+        _native.call("emsim_gb300_lens_propagate", self._plan.handle, _ptr(w), float(cs_mm), float(defocus),
+                     float(aperture), _ptr(out), nb, _stream())
+        return _wrap(out)
+
+    # -- fused image formation (extension) --------------------------------------
+    def image(self, slices, dz: float, electron_dose: float, cs_mm: float, defocus, aperture: float,
+              n_batch: Optional[int] = None, return_exit_wave: bool = False):
+        """init_wave -> multislice -> lens -> |psi|^2 in one call (pipe.py:46-55, 79-84).
+
+        ``slices``: (n_slices, n1, n2) shared or (B, n_slices, n1, n2); ``defocus``: a
+        number or a sequence (image b uses defocus[b % len]).  Returns (n1, n2) or
+        (B, n1, n2) float32 intensities (and the exit waves when requested)."""
+        n1, n2 = self.wave_shape
+        s = as_device(slices, torch.float32)
+        if s.dim() == 4:
+            nb, ns, sstride = int(s.shape[0]), int(s.shape[1]), int(s.shape[1]) * n1 * n2
+        else:
+            ns, sstride = int(s.shape[0]), 0
+            nb = n_batch or (len(defocus) if np.ndim(defocus) else 1)
+        dfs = np.atleast_1d(np.asarray(defocus, dtype=np.float64))
+        dev = _device()
+        img = torch.empty((nb, n1, n2), dtype=torch.float32, device=dev)
+        work = torch.empty((nb, n1, n2), dtype=torch.complex64, device=dev)
+        ew = torch.empty_like(work) if return_exit_wave else None
+        _native.call("emsim_gb300_multislice_image", self._plan.handle, _ptr(s), ns, sstride, float(dz),
+                     float(electron_dose), float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                     len(dfs), float(aperture), _ptr(img), _ptr(work), _ptr(ew), nb, _stream())
+        squeeze = s.dim() == 3 and n_batch is None and not np.ndim(defocus)
+        img = _wrap(img[0] if squeeze else img)
+        if return_exit_wave:
+            return img, _wrap(ew[0] if squeeze else ew)
+        return img
+
+
+def intensity(wave) -> DeviceArray:
+    """|psi|^2 of a complex64 array through the engine."""
+    w = as_device(wave, torch.complex64)
+    out = torch.empty(w.shape, dtype=torch.float32, device=w.device)
+    _native.call("emsim_gb300_intensity", _ptr(w), _ptr(out), w.numel(), _stream())
+    return _wrap(out)

@@ -1,0 +1,104 @@
+// Internal interfaces between the kernel translation units and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace emsim_gb300 {
+
+// ---------------------------------------------------------------------------
+// row passes: one CTA holds B whole rows; each row is transformed in registers/smem
+// ---------------------------------------------------------------------------
+enum RowOps : int {
+    ROW_IFFT = 1,           // inverse (unnormalised) row FFT right after the load
+    ROW_TRANSMIT = 2,       // multiply by exp(i sigma V[row, :])
+    ROW_FFT = 4,            // forward row FFT before the store
+    ROW_OUT_INTENSITY = 8,  // store |psi|^2 as float instead of complex
+    ROW_CONST_IN = 16,      // input is the constant plane wave const_val (nothing is loaded)
+};
+
+struct RowArgs {
+    const float2* in = nullptr;
+    long long in_img_stride = 0;  // float2 elements between images
+    float2* out = nullptr;
+    long long out_img_stride = 0;
+    float* out_int = nullptr;
+    long long out_int_img_stride = 0;
+    const float* slice = nullptr;  // (n1, n2) float32 per image
+    long long slice_img_stride = 0;
+    float sigma = 0.f;
+    float2 const_val = {0.f, 0.f};
+    int n_rows = 0;
+    const float2* tw = nullptr;  // FFT twiddle table of the device (twiddle_table())
+};
+
+// ---------------------------------------------------------------------------
+// column passes: one CTA holds a tile of B whole columns
+// ---------------------------------------------------------------------------
+enum ColMode : int {
+    COL_PROPAGATE = 0,  // fwd col FFT, x P(k)*band-limit/N, inverse col FFT
+    COL_LENS = 1,       // fwd col FFT, x exp(-i chi(k))*aperture*scale, inverse col FFT
+    COL_FWD = 2,        // forward col FFT only
+    COL_INV = 3,        // inverse col FFT only
+};
+
+struct ColArgs {
+    const float2* tw = nullptr;  // FFT twiddle table of the device (twiddle_table())
+    float2* data = nullptr;
+    long long img_stride = 0;
+    int n_rows = 0;  // FFT length along columns (n1)
+    int n_cols = 0;  // n2
+    // propagate: separable FP64-derived factors p1[k1] (1/N folded in), p2[k2]
+    const float2* p1 = nullptr;
+    const float2* p2 = nullptr;
+    float dfx = 0.f, dfy = 0.f;  // reference float32 frequency steps
+    float filter2 = 0.f;         // (0.6667 * fmax)^2 in float32
+    // lens: chi = f2 * (c1 * f2 - c2) in FP64; c2 = pi * lambda * defocus, one value for
+    // all images (n_c2 == 1) or one per image of the launch (n_c2 == images <= LENS_MAX)
+    double c1 = 0.0;
+    double dfx64 = 0.0, dfy64 = 0.0;
+    float aper2 = 0.f;       // (aperture / lambda)^2 in float32
+    float lens_scale = 1.f;  // normalisation folded into the transfer function
+    int n_c2 = 1;
+    double c2v[64] = {};
+};
+constexpr int LENS_MAX = 64;  // images per lens launch with distinct defocus
+
+// true when n is a power of two in [8, 4096] (the fused fast path)
+inline bool fast_len(int n) { return n >= 8 && n <= 4096 && (n & (n - 1)) == 0; }
+
+int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st);
+int launch_col(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st);
+
+// row-pass geometry actually used (rows per CTA) - exposed for tests and the autotuner
+int row_tile(int n2);
+int col_tile(int n1);
+
+// generic (any n1, n2) path: direct DFT along rows / columns + element-wise kernels
+int generic_dft_rows(const float2* in, float2* out, int n_rows, int n, bool inverse, const float2* tw_n,
+                     int n_img, cudaStream_t st);
+int generic_dft_cols(float2* data, int n_rows, int n_cols, bool inverse, const float2* tw_n, int n_img,
+                     cudaStream_t st);
+
+int ensure_twiddles(int device);
+// device address of the FFT twiddle table on the current device (after ensure_twiddles)
+const float2* twiddle_table();
+
+// opt a kernel into more than 48 KB of dynamic shared memory (once per device)
+int ensure_smem_attr(const void* func, size_t smem_bytes);
+
+// element-wise kernels (any size)
+int ew_transmit(const float2* in, const float* slice, float2* out, long long n, float sigma, int n_img,
+                long long in_stride, long long slice_stride, long long out_stride, cudaStream_t st);
+int ew_fill(float2* out, long long n, float2 value, cudaStream_t st);
+int ew_intensity(const float2* in, float* out, long long n, cudaStream_t st);
+int ew_propagate(float2* data, const ColArgs& a, int n_img, cudaStream_t st);
+int ew_lens(float2* data, const ColArgs& a, int n_img, cudaStream_t st);
+int prop_tables(float2* p1, float2* p2, int n1, int n2, double dfx64, double dfy64, double phase_coef,
+                double inv_n, cudaStream_t st);
+
+}  // namespace emsim_gb300

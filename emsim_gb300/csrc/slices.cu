@@ -1,0 +1,363 @@
+// Slice-builder plan, atom binning and the generic (any size) slice build, with their
+// C-ABI entry points (include/emsim_gb300.h).
+//
+// Replaces emsim::cuda::OneSliceBuilder / MultiSlicesBuilder
+// (emsim/backend/cuda_ext/src/SliceBuilder.cu, SliceBuilder_kernel.cu) and the cupy
+// band-limit + clip of emsim/backend/slice_builder_cuda.py:39-70, 88-99.
+#include <cmath>
+#include <vector>
+
+#include "slices.h"
+
+using namespace emsim_gb300;
+
+struct emsim_gb300_slice_plan {
+    int n_elems = 0, n_slices = 0, n1 = 0, n2 = 0;
+    double dz = 0, d1 = 0, d2 = 0;
+    bool fast = false;
+    int device = 0;
+    const float2* tw = nullptr;
+    float2* tw1 = nullptr;  // generic path twiddles exp(-2 pi i m / n)
+    float2* tw2 = nullptr;
+    float* filt = nullptr;  // (n_elems, n1, n2): F(k) * SF_e(k) / N
+};
+
+namespace {
+
+int check_device(const emsim_gb300_slice_plan* p) {
+    EMSIM_REQUIRE(p != nullptr, EMSIM_GB300_ERR_INVALID, "null slice plan");
+    int dev = -1;
+    EMSIM_CHECK_CUDA(cudaGetDevice(&dev));
+    EMSIM_REQUIRE(dev == p->device, EMSIM_GB300_ERR_DEVICE, "slice plan used on a device other than its own");
+    return EMSIM_GB300_OK;
+}
+
+// numpy floor division (Python semantics) for the centred band-limit grid
+inline int py_floordiv(int a, int b) {
+    int q = a / b;
+    if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
+    return q;
+}
+
+// Full-spectrum real filter F(k) equivalent to the reference band-limit
+// irfft2(rfft2(V) * fil[:, :n2//2+1]) (slice_builder_cuda.py:88-99): fil is the disc
+// k1^2 + k2^2 <= (min(n1,n2)//2)^2 on numpy's centred grid arange(-n//2, -n//2 + n),
+// ifftshifted.  C2R weights the stored half spectrum by w = 1 on self-conjugate
+// columns and 2 elsewhere; for a real input this equals applying the symmetric
+// F(k) = (G(k) + G(-k)) / 2 with G = w * fil on the half spectrum and 0 beyond it.
+std::vector<float> bandlimit_full(int n1, int n2) {
+    const int r = (n1 < n2 ? n1 : n2) / 2;
+    auto centred = [](int i, int n) { return ((i + n / 2) % n) + py_floordiv(-n, 2); };
+    const int h2 = n2 / 2;
+    auto G = [&](int i, int j) -> double {
+        if (j > h2) return 0.0;
+        const int c1 = centred(i, n1), c2 = centred(j, n2);
+        const double fil = ((long long)c1 * c1 + (long long)c2 * c2 <= (long long)r * r) ? 1.0 : 0.0;
+        const bool selfconj = (j == 0) || (n2 % 2 == 0 && j == h2);
+        return (selfconj ? 1.0 : 2.0) * fil;
+    };
+    std::vector<float> F((size_t)n1 * n2);
+    for (int i = 0; i < n1; ++i)
+        for (int j = 0; j < n2; ++j) {
+            const int mi = (n1 - i) % n1, mj = (n2 - j) % n2;
+            F[(size_t)i * n2 + j] = (float)(0.5 * (G(i, j) + G(mi, mj)));
+        }
+    return F;
+}
+
+int make_tw(int n, float2** out) {
+    std::vector<float2> h(n);
+    for (int m = 0; m < n; ++m) {
+        const double a = -2.0 * M_PI * (double)m / (double)n;
+        h[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    EMSIM_CHECK_CUDA(cudaMalloc((void**)out, sizeof(float2) * n));
+    EMSIM_CHECK_CUDA(cudaMemcpy(*out, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    return EMSIM_GB300_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// binning (CUDA rule of SliceBuilder_kernel.cu:9-123)
+// ---------------------------------------------------------------------------------
+struct BinAxis {
+    float start, end, d;
+    int n;
+};
+
+// start = -d * floorf((float)(n + 1) / 2.0f); end = start + (float)n * d, which nvcc
+// contracts into one fused multiply-add (SliceBuilder_kernel.cu:30-34, 87-92).
+BinAxis make_axis(int n, double d) {
+    BinAxis a;
+    a.d = (float)d;
+    const float half = std::floor((float)(n + 1) / 2.0f);
+    a.start = -a.d * half;
+    a.end = std::fma((float)n, a.d, a.start);
+    a.n = n;
+    return a;
+}
+
+__device__ __forceinline__ bool bin_axis(float x, const BinAxis& ax, int& idx) {
+    if (!(ax.start <= x && x <= ax.end)) return false;
+    // LEFT_CLOSE: float difference compared against the double literal 1e-12
+    if ((double)__fsub_rn(ax.end, x) < 1e-12) {
+        idx = ax.n - 1;
+    } else {
+        int i = (int)floorf(__fdiv_rn(__fsub_rn(x, ax.start), ax.d));
+        // x a hair below end can round up to n; the reference then writes past the row
+        idx = i < ax.n ? i : ax.n - 1;
+    }
+    return true;
+}
+
+constexpr int MAX_ELEMS = 128;
+
+// One thread per atom.  Element of row r = number of cumulative counts <= r.  Counts
+// accumulate as exact integers: float atomics of 1.0f while every bin stays below 2^24
+// (guaranteed for n_atoms < 2^24), unsigned atomics plus a conversion pass otherwise, so
+// the histogram never depends on execution order.
+template <bool THREE_D, bool U32>
+__global__ void bin_kernel(const float* __restrict__ coords, unsigned n_atoms, const uint32_t* __restrict__ counts,
+                           int n_elems, BinAxis a0, BinAxis a1, BinAxis a2, float* out) {
+    __shared__ unsigned long long cum[MAX_ELEMS];
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int e = 0; e < n_elems; ++e) {
+            s += counts[e];
+            cum[e] = s;
+        }
+    }
+    __syncthreads();
+    const long long plane = (long long)a1.n * a2.n;
+    const long long vol = THREE_D ? plane * a0.n : plane;
+    for (unsigned r = blockIdx.x * blockDim.x + threadIdx.x; r < n_atoms; r += gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_elems;  // first e with cum[e] > r
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (cum[mid] > r) hi = mid;
+            else lo = mid + 1;
+        }
+        if (lo >= n_elems) continue;  // rows beyond sum(counts) belong to no element
+        const float z = coords[3ull * r + 0], x = coords[3ull * r + 1], y = coords[3ull * r + 2];
+        int i = 0, j = 0, k = 0;
+        long long lin;
+        if (THREE_D) {
+            if (!bin_axis(z, a0, i) || !bin_axis(x, a1, j) || !bin_axis(y, a2, k)) continue;
+            lin = (long long)lo * vol + (long long)i * plane + (long long)j * a2.n + k;
+        } else {
+            if (!bin_axis(x, a1, j) || !bin_axis(y, a2, k)) continue;
+            lin = (long long)lo * vol + (long long)j * a2.n + k;
+        }
+        if (U32) atomicAdd(reinterpret_cast<unsigned*>(out) + lin, 1u);
+        else atomicAdd(out + lin, 1.0f);
+    }
+}
+
+__global__ void u32_to_f32_kernel(float* data, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        data[i] = (float)reinterpret_cast<unsigned*>(data)[i];
+}
+
+int bin_atoms(emsim_gb300_slice_plan* p, const float* coords, unsigned n_atoms, const uint32_t* counts, float* out,
+              bool three_d, cudaStream_t st) {
+    EMSIM_TRY(check_device(p));
+    EMSIM_REQUIRE(out && (n_atoms == 0 || (coords && counts)), EMSIM_GB300_ERR_INVALID, "bin_atoms: bad arguments");
+    EMSIM_REQUIRE(p->n_elems <= MAX_ELEMS, EMSIM_GB300_ERR_UNSUPPORTED, "bin_atoms: more than 128 elements");
+    const long long plane = (long long)p->n1 * p->n2;
+    const long long total = (three_d ? plane * p->n_slices : plane) * p->n_elems;
+    EMSIM_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * total, st));
+    if (n_atoms == 0) return EMSIM_GB300_OK;
+    const BinAxis a0 = make_axis(p->n_slices, p->dz), a1 = make_axis(p->n1, p->d1), a2 = make_axis(p->n2, p->d2);
+    int blocks = ceil_div(n_atoms, 256);
+    if (blocks > 65535) blocks = 65535;
+    const bool u32 = n_atoms >= (1u << 24);
+    if (three_d) {
+        if (u32) bin_kernel<true, true><<<blocks, 256, 0, st>>>(coords, n_atoms, counts, p->n_elems, a0, a1, a2, out);
+        else bin_kernel<true, false><<<blocks, 256, 0, st>>>(coords, n_atoms, counts, p->n_elems, a0, a1, a2, out);
+    } else {
+        if (u32) bin_kernel<false, true><<<blocks, 256, 0, st>>>(coords, n_atoms, counts, p->n_elems, a0, a1, a2, out);
+        else bin_kernel<false, false><<<blocks, 256, 0, st>>>(coords, n_atoms, counts, p->n_elems, a0, a1, a2, out);
+    }
+    EMSIM_CHECK_LAUNCH();
+    if (u32) {
+        int cb = ceil_div(total, 256);
+        if (cb > 8192) cb = 8192;
+        u32_to_f32_kernel<<<cb, 256, 0, st>>>(out, total);
+        EMSIM_CHECK_LAUNCH();
+    }
+    return EMSIM_GB300_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// generic (any size) slice build: same algebra with direct DFTs
+// ---------------------------------------------------------------------------------
+__global__ void pack_pairs_kernel(SliceArgs a) {
+    const long long npix = (long long)a.n1 * a.n2;
+    const int img = blockIdx.y;
+    const int e = img / a.n_pairs, pair = img - e * a.n_pairs;
+    const int s0 = 2 * pair, s1 = 2 * pair + 1;
+    const float* h0 = a.hist + ((long long)e * a.n_slices + s0) * npix;
+    const float* h1 = s1 < a.n_slices ? a.hist + ((long long)e * a.n_slices + s1) * npix : nullptr;
+    float2* z = a.work + (long long)img * npix;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix; i += (long long)gridDim.x * blockDim.x)
+        z[i] = make_float2(h0[i], h1 ? h1[i] : 0.f);
+}
+
+__global__ void element_sum_kernel(SliceArgs a) {
+    const long long npix = (long long)a.n1 * a.n2;
+    const int pair = blockIdx.y;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix; i += (long long)gridDim.x * blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int e = 0; e < a.n_elems; ++e) {
+            const float2 z = a.work[((long long)e * a.n_pairs + pair) * npix + i];
+            const float w = a.filt[(long long)e * npix + i];
+            acc.x = fmaf(w, z.x, acc.x);
+            acc.y = fmaf(w, z.y, acc.y);
+        }
+        a.work[(long long)pair * npix + i] = acc;
+    }
+}
+
+__global__ void unpack_clip_kernel(SliceArgs a) {
+    const long long npix = (long long)a.n1 * a.n2;
+    const int pair = blockIdx.y;
+    const int s0 = 2 * pair, s1 = 2 * pair + 1;
+    const float2* w = a.work + (long long)pair * npix;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix; i += (long long)gridDim.x * blockDim.x) {
+        const float2 v = w[i];
+        a.out[(long long)s0 * npix + i] = v.x < 1e-13f ? 1e-13f : v.x;
+        if (s1 < a.n_slices) a.out[(long long)s1 * npix + i] = v.y < 1e-13f ? 1e-13f : v.y;
+    }
+}
+
+int generic_build(emsim_gb300_slice_plan* p, const SliceArgs& a, cudaStream_t st) {
+    const long long npix = (long long)p->n1 * p->n2;
+    int blocks = ceil_div(npix, 256);
+    if (blocks > 2048) blocks = 2048;
+    const int nz = a.n_elems * a.n_pairs;
+    pack_pairs_kernel<<<dim3(blocks, nz), 256, 0, st>>>(a);
+    EMSIM_CHECK_LAUNCH();
+    EMSIM_TRY(generic_dft_rows(a.work, a.work, p->n1, p->n2, false, p->tw2, nz, st));
+    EMSIM_TRY(generic_dft_cols(a.work, p->n1, p->n2, false, p->tw1, nz, st));
+    element_sum_kernel<<<dim3(blocks, a.n_pairs), 256, 0, st>>>(a);
+    EMSIM_CHECK_LAUNCH();
+    EMSIM_TRY(generic_dft_cols(a.work, p->n1, p->n2, true, p->tw1, a.n_pairs, st));
+    EMSIM_TRY(generic_dft_rows(a.work, a.work, p->n1, p->n2, true, p->tw2, a.n_pairs, st));
+    unpack_clip_kernel<<<dim3(blocks, a.n_pairs), 256, 0, st>>>(a);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int emsim_gb300_slice_plan_create(const float* sf_half, int n_elems, int n_slices, int n1, int n2, double dz,
+                                  double d1, double d2, int symmetric_bandlimit, emsim_gb300_slice_plan** plan) {
+    EMSIM_REQUIRE(plan != nullptr, EMSIM_GB300_ERR_INVALID, "null plan output pointer");
+    *plan = nullptr;
+    EMSIM_REQUIRE(n_elems >= 1 && n_slices >= 1 && n1 >= 1 && n2 >= 1, EMSIM_GB300_ERR_INVALID,
+                  "slice plan: sizes must be positive");
+    EMSIM_REQUIRE(sf_half != nullptr, EMSIM_GB300_ERR_INVALID, "slice plan: null scattering factors");
+    EMSIM_REQUIRE(d1 > 0 && d2 > 0 && dz > 0, EMSIM_GB300_ERR_INVALID, "slice plan: steps must be positive");
+    EMSIM_REQUIRE(n1 <= 16384 && n2 <= 16384, EMSIM_GB300_ERR_UNSUPPORTED, "slice plan: side above 16384");
+    auto* p = new emsim_gb300_slice_plan();
+    p->n_elems = n_elems;
+    p->n_slices = n_slices;
+    p->n1 = n1;
+    p->n2 = n2;
+    p->dz = dz;
+    p->d1 = d1;
+    p->d2 = d2;
+    p->fast = fast_len(n1) && fast_len(n2);
+    auto fail = [&](int code) {
+        cudaFree(p->tw1);
+        cudaFree(p->tw2);
+        cudaFree(p->filt);
+        delete p;
+        return code;
+    };
+    if (cudaGetDevice(&p->device) != cudaSuccess) {
+        set_error("cudaGetDevice failed");
+        return fail(EMSIM_GB300_ERR_CUDA);
+    }
+    int st;
+    if ((st = ensure_twiddles(p->device)) != EMSIM_GB300_OK) return fail(st);
+    p->tw = twiddle_table();
+    if (!p->fast) {
+        if ((st = make_tw(n1, &p->tw1)) != EMSIM_GB300_OK) return fail(st);
+        if ((st = make_tw(n2, &p->tw2)) != EMSIM_GB300_OK) return fail(st);
+    }
+    // T_e(k) = F(k) * SF_e(k) / N on the full spectrum; SF_e(k) = SF_e(-k) supplies the
+    // columns beyond n2/2 from the stored half spectrum.
+    const std::vector<float> F =
+        symmetric_bandlimit ? bandlimit_full(n1, n2) : std::vector<float>((size_t)n1 * n2, 1.0f);
+    const int h = n2 / 2 + 1;
+    const double inv_n = 1.0 / ((double)n1 * (double)n2);
+    std::vector<float> T((size_t)n_elems * n1 * n2);
+    for (int e = 0; e < n_elems; ++e)
+        for (int i = 0; i < n1; ++i)
+            for (int j = 0; j < n2; ++j) {
+                const float sf = j < h ? sf_half[((size_t)e * n1 + i) * h + j]
+                                       : sf_half[((size_t)e * n1 + (n1 - i) % n1) * h + (n2 - j)];
+                T[((size_t)e * n1 + i) * n2 + j] = (float)((double)F[(size_t)i * n2 + j] * (double)sf * inv_n);
+            }
+    if (cudaMalloc((void**)&p->filt, sizeof(float) * T.size()) != cudaSuccess ||
+        cudaMemcpy(p->filt, T.data(), sizeof(float) * T.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("slice plan: filter upload failed");
+        return fail(EMSIM_GB300_ERR_CUDA);
+    }
+    *plan = p;
+    return EMSIM_GB300_OK;
+}
+
+int emsim_gb300_slice_plan_destroy(emsim_gb300_slice_plan* p) {
+    if (!p) return EMSIM_GB300_OK;
+    cudaFree(p->tw1);
+    cudaFree(p->tw2);
+    cudaFree(p->filt);
+    delete p;
+    return EMSIM_GB300_OK;
+}
+
+int emsim_gb300_bin_atoms_one_slice(emsim_gb300_slice_plan* p, const float* coords, unsigned n_atoms,
+                                    const uint32_t* counts, float* out, void* stream) {
+    return bin_atoms(p, coords, n_atoms, counts, out, false, (cudaStream_t)stream);
+}
+
+int emsim_gb300_bin_atoms_multi_slices(emsim_gb300_slice_plan* p, const float* coords, unsigned n_atoms,
+                                       const uint32_t* counts, float* out, void* stream) {
+    return bin_atoms(p, coords, n_atoms, counts, out, true, (cudaStream_t)stream);
+}
+
+size_t emsim_gb300_make_slices_workspace_size(const emsim_gb300_slice_plan* p) {
+    if (!p) return 0;
+    const size_t pairs = (size_t)(p->n_slices + 1) / 2;
+    return sizeof(float2) * (size_t)p->n_elems * pairs * p->n1 * p->n2;
+}
+
+int emsim_gb300_make_slices(emsim_gb300_slice_plan* p, const float* hist, float* out, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+    EMSIM_TRY(check_device(p));
+    EMSIM_REQUIRE(hist && out && workspace, EMSIM_GB300_ERR_INVALID, "make_slices: null pointer");
+    EMSIM_REQUIRE(workspace_bytes >= emsim_gb300_make_slices_workspace_size(p), EMSIM_GB300_ERR_INVALID,
+                  "make_slices: workspace too small");
+    EMSIM_REQUIRE(((uintptr_t)workspace & 255) == 0, EMSIM_GB300_ERR_INVALID, "make_slices: workspace not 256-byte aligned");
+    SliceArgs a;
+    a.hist = hist;
+    a.out = out;
+    a.work = (float2*)workspace;
+    a.filt = p->filt;
+    a.tw = p->tw;
+    a.n_elems = p->n_elems;
+    a.n_slices = p->n_slices;
+    a.n_pairs = (p->n_slices + 1) / 2;
+    a.n1 = p->n1;
+    a.n2 = p->n2;
+    EMSIM_REQUIRE((long long)a.n_elems * a.n_pairs <= 65535, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "make_slices: more than 65535 element x slice-pair planes");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (p->fast) return slice_fast_build(a, st);
+    return generic_build(p, a, st);
+}
+
+}  // extern "C"

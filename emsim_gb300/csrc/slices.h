@@ -1,0 +1,19 @@
+// Internal interface of the slice builder (binning + projected-potential slices).
+#pragma once
+
+#include "engine.h"
+
+namespace emsim_gb300 {
+
+struct SliceArgs {
+    const float* hist = nullptr;  // (n_elems, n_slices, n1, n2)
+    float* out = nullptr;         // (n_slices, n1, n2)
+    float2* work = nullptr;       // (n_elems, n_pairs, n1, n2) complex
+    const float* filt = nullptr;  // (n_elems, n1, n2) real: band-limit * SF_e / N
+    const float2* tw = nullptr;   // FFT twiddle table of the device
+    int n_elems = 0, n_slices = 0, n_pairs = 0, n1 = 0, n2 = 0;
+};
+
+int slice_fast_build(const SliceArgs& a, cudaStream_t st);
+
+}  // namespace emsim_gb300

@@ -1,0 +1,301 @@
+// Size dispatch of the fused passes, the twiddle table, the generic (any-size) path and
+// the element-wise kernels of the wave propagator.
+#include <mutex>
+#include <set>
+#include <utility>
+
+#include "wave_passes.cuh"
+
+namespace emsim_gb300 {
+
+// exp(-2 pi i m / TW_SIZE); one copy per device, written once by init_twiddle_kernel
+static __device__ float2 g_twiddle[fft::TW_SIZE];
+
+// ---------------------------------------------------------------------------------
+// error string (per host thread)
+// ---------------------------------------------------------------------------------
+static thread_local std::string t_last_error;
+void set_error(const std::string& msg) { t_last_error = msg; }
+const char* get_error() { return t_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------------
+// one-time per-device state
+// ---------------------------------------------------------------------------------
+__global__ void init_twiddle_kernel() {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < fft::TW_SIZE) {
+        double s, c;
+        sincospi(-2.0 * (double)m / (double)fft::TW_SIZE, &s, &c);
+        g_twiddle[m] = make_float2((float)c, (float)s);
+    }
+}
+
+static std::mutex g_init_mu;
+static std::set<int> g_twiddle_ready;
+static const float2* g_twiddle_addr[64] = {};
+static std::set<std::pair<int, const void*>> g_smem_ready;
+
+// The table is written by a kernel on the legacy default stream and waited for, so it is
+// visible to every stream of the device afterwards.  Called from plan creation.
+int ensure_twiddles(int device) {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (g_twiddle_ready.count(device)) return EMSIM_GB300_OK;
+    EMSIM_REQUIRE(device >= 0 && device < 64, EMSIM_GB300_ERR_UNSUPPORTED, "device index above 63");
+    init_twiddle_kernel<<<fft::TW_SIZE / 256, 256>>>();
+    EMSIM_CHECK_LAUNCH();
+    EMSIM_CHECK_CUDA(cudaDeviceSynchronize());
+    void* addr = nullptr;
+    EMSIM_CHECK_CUDA(cudaGetSymbolAddress(&addr, g_twiddle));
+    g_twiddle_addr[device] = (const float2*)addr;
+    g_twiddle_ready.insert(device);
+    return EMSIM_GB300_OK;
+}
+
+const float2* twiddle_table() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    return g_twiddle_addr[dev];
+}
+
+int ensure_smem_attr(const void* func, size_t smem_bytes) {
+    if (smem_bytes <= 48 * 1024) return EMSIM_GB300_OK;
+    int dev = 0;
+    EMSIM_CHECK_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    auto key = std::make_pair(dev, func);
+    if (g_smem_ready.count(key)) return EMSIM_GB300_OK;
+    EMSIM_CHECK_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    g_smem_ready.insert(key);
+    return EMSIM_GB300_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// fast-path dispatch
+// ---------------------------------------------------------------------------------
+#define EMSIM_FAST_SIZES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
+#define EMSIM_DECL(N)                                                                  \
+    extern template int launch_row_n<N>(int, const RowArgs&, int, cudaStream_t);       \
+    extern template int launch_col_n<N>(int, const ColArgs&, int, cudaStream_t);
+EMSIM_FAST_SIZES(EMSIM_DECL)
+#undef EMSIM_DECL
+
+int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
+    switch (n2) {
+#define EMSIM_CASE(N) \
+    case N: return launch_row_n<N>(ops, a, n_img, st);
+        EMSIM_FAST_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
+    }
+    set_error("row pass: length not on the fast path");
+    return EMSIM_GB300_ERR_UNSUPPORTED;
+}
+
+int launch_col(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st) {
+    switch (n1) {
+#define EMSIM_CASE(N) \
+    case N: return launch_col_n<N>(mode, a, n_img, st);
+        EMSIM_FAST_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
+    }
+    set_error("column pass: length not on the fast path");
+    return EMSIM_GB300_ERR_UNSUPPORTED;
+}
+
+int row_tile(int n2) {
+    int B = row_threads(n2) / (n2 / 8);
+    return B;
+}
+int col_tile(int n1) { return col_B_for(n1, 1 << 30); }
+
+// ---------------------------------------------------------------------------------
+// generic path: direct DFT (O(n^2) per line) for lengths off the fast path
+// ---------------------------------------------------------------------------------
+// tw_n[m] = exp(-2 pi i m / n), m < n (FP64-derived).  One CTA per line.
+__global__ void dft_rows_kernel(const float2* in, float2* out, int n_rows, int n, int inverse,
+                                const float2* __restrict__ tw, long long img_stride) {
+    extern __shared__ float2 line[];
+    const long long img = blockIdx.y;
+    const long long off = img * img_stride + (long long)blockIdx.x * n;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) line[j] = in[off + j];
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        long long idx = 0;
+        for (int j = 0; j < n; ++j) {
+            float2 w = __ldg(tw + idx);
+            if (inverse) w.y = -w.y;
+            acc = cadd(acc, cmul(line[j], w));
+            idx += k;
+            if (idx >= n) idx -= n;
+        }
+        // every thread has read the whole row into smem before any write (in-place safe)
+        out[off + k] = acc;
+    }
+}
+
+__global__ void dft_cols_kernel(float2* data, int n_rows, int n_cols, int inverse,
+                                const float2* __restrict__ tw, long long img_stride) {
+    extern __shared__ float2 line[];
+    const long long img = blockIdx.y;
+    float2* base = data + img * img_stride + blockIdx.x;
+    const int n = n_rows;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) line[j] = base[(long long)j * n_cols];
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        long long idx = 0;
+        for (int j = 0; j < n; ++j) {
+            float2 w = __ldg(tw + idx);
+            if (inverse) w.y = -w.y;
+            acc = cadd(acc, cmul(line[j], w));
+            idx += k;
+            if (idx >= n) idx -= n;
+        }
+        // every thread has read the whole column into smem before any write
+        base[(long long)k * n_cols] = acc;
+    }
+}
+
+int generic_dft_rows(const float2* in, float2* out, int n_rows, int n, bool inverse, const float2* tw_n,
+                     int n_img, cudaStream_t st) {
+    const size_t smem = (size_t)n * sizeof(float2);
+    EMSIM_TRY(ensure_smem_attr((const void*)dft_rows_kernel, smem));
+    dft_rows_kernel<<<dim3(n_rows, n_img), 256, smem, st>>>(in, out, n_rows, n, inverse ? 1 : 0, tw_n,
+                                                            (long long)n_rows * n);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+int generic_dft_cols(float2* data, int n_rows, int n_cols, bool inverse, const float2* tw_n, int n_img,
+                     cudaStream_t st) {
+    const size_t smem = (size_t)n_rows * sizeof(float2);
+    EMSIM_TRY(ensure_smem_attr((const void*)dft_cols_kernel, smem));
+    dft_cols_kernel<<<dim3(n_cols, n_img), 256, smem, st>>>(data, n_rows, n_cols, inverse ? 1 : 0, tw_n,
+                                                            (long long)n_rows * n_cols);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// element-wise kernels
+// ---------------------------------------------------------------------------------
+__global__ void transmit_kernel(const float2* in, const float* __restrict__ slice, float2* out, long long n,
+                                float sigma, long long in_stride, long long slice_stride, long long out_stride) {
+    const long long img = blockIdx.y;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float s, c;
+        sincosf(sigma * slice[img * slice_stride + i], &s, &c);
+        out[img * out_stride + i] = cmul(in[img * in_stride + i], make_float2(c, s));
+    }
+}
+
+int ew_transmit(const float2* in, const float* slice, float2* out, long long n, float sigma, int n_img,
+                long long in_stride, long long slice_stride, long long out_stride, cudaStream_t st) {
+    int blocks = ceil_div(n, 256);
+    if (blocks > 4096) blocks = 4096;
+    transmit_kernel<<<dim3(blocks, n_img), 256, 0, st>>>(in, slice, out, n, sigma, in_stride, slice_stride,
+                                                         out_stride);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+__global__ void fill_kernel(float2* out, long long n, float2 value) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = value;
+}
+
+int ew_fill(float2* out, long long n, float2 value, cudaStream_t st) {
+    int blocks = ceil_div(n, 256);
+    if (blocks > 8192) blocks = 8192;
+    fill_kernel<<<blocks, 256, 0, st>>>(out, n, value);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+__global__ void intensity_kernel(const float2* __restrict__ in, float* __restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 v = in[i];
+        out[i] = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
+    }
+}
+
+int ew_intensity(const float2* in, float* out, long long n, cudaStream_t st) {
+    int blocks = ceil_div(n, 256);
+    if (blocks > 8192) blocks = 8192;
+    intensity_kernel<<<blocks, 256, 0, st>>>(in, out, n);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+// full-spectrum multiply by P(k) * band-limit (p1 carries 1/N), for the generic path
+__global__ void propagate_kernel(float2* data, ColArgs a) {
+    const long long n = (long long)a.n_rows * a.n_cols;
+    const long long img = blockIdx.y;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(i / a.n_cols), c = (int)(i - (long long)r * a.n_cols);
+        const float f2 = freq_sq_ref(fftfreq_int(r, a.n_rows), fftfreq_int(c, a.n_cols), a.dfx, a.dfy);
+        float2* p = data + img * a.img_stride + i;
+        *p = (f2 <= a.filter2) ? cmul(*p, cmul(a.p1[r], a.p2[c])) : make_float2(0.f, 0.f);
+    }
+}
+
+int ew_propagate(float2* data, const ColArgs& a, int n_img, cudaStream_t st) {
+    int blocks = ceil_div((long long)a.n_rows * a.n_cols, 256);
+    if (blocks > 4096) blocks = 4096;
+    propagate_kernel<<<dim3(blocks, n_img), 256, 0, st>>>(data, a);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+__global__ void lens_kernel(float2* data, ColArgs a) {
+    const long long n = (long long)a.n_rows * a.n_cols;
+    const long long img = blockIdx.y;
+    const double c2 = a.c2v[a.n_c2 > 1 ? img : 0];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(i / a.n_cols), c = (int)(i - (long long)r * a.n_cols);
+        const int k2 = fftfreq_int(c, a.n_cols);
+        const double fy = (double)k2 * a.dfy64;
+        float2* p = data + img * a.img_stride + i;
+        *p = cmul(*p, lens_factor(fftfreq_int(r, a.n_rows), k2, fy * fy, c2, a));
+    }
+}
+
+int ew_lens(float2* data, const ColArgs& a, int n_img, cudaStream_t st) {
+    int blocks = ceil_div((long long)a.n_rows * a.n_cols, 256);
+    if (blocks > 4096) blocks = 4096;
+    lens_kernel<<<dim3(blocks, n_img), 256, 0, st>>>(data, a);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+// p1[k1] = exp(-i phase_coef fx^2) * inv_n, p2[k2] = exp(-i phase_coef fy^2);
+// phase_coef = pi * lambda * dz.  The phase is formed and reduced mod 2 pi in FP64.
+__global__ void prop_table_kernel(float2* p1, float2* p2, int n1, int n2, double dfx64, double dfy64,
+                                  double phase_coef, double inv_n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n1 + n2) {
+        const bool first = i < n1;
+        const int k = first ? fftfreq_int(i, n1) : fftfreq_int(i - n1, n2);
+        const double f = (double)k * (first ? dfx64 : dfy64);
+        double ph = phase_coef * f * f;
+        ph = fma(-TWO_PI, rint(ph * INV_TWO_PI), ph);
+        float s, c;
+        sincosf((float)ph, &s, &c);
+        const float sc = first ? (float)inv_n : 1.f;
+        const float2 v = make_float2(c * sc, -s * sc);
+        if (first) p1[i] = v;
+        else p2[i - n1] = v;
+    }
+}
+
+int prop_tables(float2* p1, float2* p2, int n1, int n2, double dfx64, double dfy64, double phase_coef,
+                double inv_n, cudaStream_t st) {
+    prop_table_kernel<<<ceil_div(n1 + n2, 256), 256, 0, st>>>(p1, p2, n1, n2, dfx64, dfy64, phase_coef, inv_n);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
+}  // namespace emsim_gb300
+
+extern "C" const char* emsim_gb300_last_error(void) { return emsim_gb300::get_error(); }
+extern "C" int emsim_gb300_abi_version(void) { return EMSIM_GB300_ABI_VERSION; }

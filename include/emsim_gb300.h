@@ -1,0 +1,146 @@
+/*
+ * emsim_gb300 - C ABI of the GB300 (sm_103a) multislice engine for emsim.
+ *
+ * Plain pointers and sizes only.  Device pointers point to CUDA global memory on the
+ * device that was current when the plan was created; "stream" is a cudaStream_t passed
+ * as void* (NULL = legacy default stream).  Complex arrays are interleaved float32
+ * (re, im) pairs, row-major, C-contiguous, exactly the cufftComplex layout the reference
+ * extension uses.  Every entry point returns EMSIM_GB300_OK (0) or an error code; the
+ * message of the last failure on the calling thread is returned by
+ * emsim_gb300_last_error().  Work is enqueued asynchronously on "stream"; nothing here
+ * synchronises the device except plan creation.
+ *
+ * Reference interfaces replaced (paths inside the emsim project):
+ *   emsim::cuda::WavePropagator    emsim/backend/cuda_ext/src/WavePropagator.h:15-41,
+ *                                  pybind wrapper wave_kernel_cuda.cpp:28-143
+ *   emsim::cuda::OneSliceBuilder   emsim/backend/cuda_ext/src/SliceBuilder.h,
+ *   emsim::cuda::MultiSlicesBuilder  pybind wrapper slice_kernel_cuda.cpp:80-214
+ */
+#ifndef EMSIM_GB300_H
+#define EMSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EMSIM_GB300_ABI_VERSION 1
+
+enum {
+    EMSIM_GB300_OK = 0,
+    EMSIM_GB300_ERR_INVALID = 1,     /* bad argument (null pointer, size, shape) */
+    EMSIM_GB300_ERR_CUDA = 2,        /* CUDA runtime error (message has details) */
+    EMSIM_GB300_ERR_UNSUPPORTED = 3, /* valid request this build does not handle */
+    EMSIM_GB300_ERR_DEVICE = 4       /* plan used on a device other than its own */
+};
+
+typedef struct emsim_gb300_wave_plan emsim_gb300_wave_plan;
+typedef struct emsim_gb300_slice_plan emsim_gb300_slice_plan;
+
+/* ABI version (EMSIM_GB300_ABI_VERSION). */
+int emsim_gb300_abi_version(void);
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char* emsim_gb300_last_error(void);
+
+/* ---------------------------------------------------------------------------------
+ * Wave propagator.  Replaces WavePropagator(n1, n2, d1, d2, waveLength,
+ * relativityGamma) (cuda_ext/src/WavePropagator.cu:14-21; python side
+ * backend/wave_propagator_cuda.py:26-31).  wave_length in Angstrom, relativity_gamma
+ * dimensionless (both FP64; sigma = gamma * lambda is formed in FP64).
+ * All wave operations below take n_batch >= 1 images of shape (n1, n2) stored
+ * back to back; input and output may alias (in-place).
+ * ------------------------------------------------------------------------------- */
+int emsim_gb300_wave_plan_create(int n1, int n2, double d1, double d2, double wave_length,
+                                 double relativity_gamma, emsim_gb300_wave_plan** plan);
+int emsim_gb300_wave_plan_destroy(emsim_gb300_wave_plan* plan);
+
+/* psi = sqrt(dose * d1 * d2) everywhere (wave_propagator_base.py:25-29). */
+int emsim_gb300_init_wave(emsim_gb300_wave_plan* plan, double electron_dose, void* wave_out,
+                          int n_batch, void* stream);
+
+/* psi * exp(i sigma V) (WavePropagator.cu:27-29, kernel WavePropagator_kernel.cu:12-43).
+ * slice: (n1, n2) float32, shared by all images when slice_batch_stride == 0, else
+ * slice_batch_stride floats apart. */
+int emsim_gb300_slice_transmit(emsim_gb300_wave_plan* plan, const void* wave, const float* slice,
+                               long long slice_batch_stride, void* wave_out, int n_batch, void* stream);
+
+/* IFFT(P(dz) * bandlimit * FFT(psi)) / N (WavePropagator.cu:32-42,
+ * kernel WavePropagator_kernel.cu:46-94). */
+int emsim_gb300_space_propagate(emsim_gb300_wave_plan* plan, const void* wave, double dz, void* wave_out,
+                                int n_batch, void* stream);
+
+/* transmit then space-propagate (WavePropagator.cu:56-60). */
+int emsim_gb300_singleslice_propagate(emsim_gb300_wave_plan* plan, const void* wave, const float* slice,
+                                      long long slice_batch_stride, double dz, void* wave_out, int n_batch,
+                                      void* stream);
+
+/* the multislice loop over slices (n_slices, n1, n2) float32 (WavePropagator.cu:62-70).
+ * slices_batch_stride: floats between the slice stacks of consecutive images (0 = shared). */
+int emsim_gb300_multislice_propagate(emsim_gb300_wave_plan* plan, const void* wave, const float* slices,
+                                     int n_slices, long long slices_batch_stride, double dz, void* wave_out,
+                                     int n_batch, void* stream);
+
+/* objective lens: IFFT(exp(-i chi) * aperture * FFT(psi)) / N
+ * (WavePropagator.cu:44-54, kernel WavePropagator_kernel.cu:97-145). */
+int emsim_gb300_lens_propagate(emsim_gb300_wave_plan* plan, const void* wave, double cs_mm, double defocus,
+                               double aperture, void* wave_out, int n_batch, void* stream);
+
+/* |psi|^2 (pipe.py:81-82). n = number of complex elements. */
+int emsim_gb300_intensity(const void* wave, float* intensity_out, long long n, void* stream);
+
+/* Fused image formation for n_batch images (pipe.py:46-55, 79-84 after the slices exist):
+ * init_wave(dose) -> multislice over (n_slices, n1, n2) -> lens -> |psi|^2.  The plane
+ * wave is generated in registers and the exit wave is only written when
+ * exit_wave_out != NULL.  defocus_host: n_defocus values in host memory; image b uses
+ * defocus_host[b % n_defocus] and slice stack b * slices_batch_stride.
+ * wave_work: device scratch of n_batch * n1 * n2 complex64 (contents undefined on
+ * return); image_out: (n_batch, n1, n2) float32. */
+int emsim_gb300_multislice_image(emsim_gb300_wave_plan* plan, const float* slices, int n_slices,
+                                 long long slices_batch_stride, double dz, double electron_dose, double cs_mm,
+                                 const double* defocus_host, int n_defocus, double aperture, float* image_out,
+                                 void* wave_work, void* exit_wave_out, int n_batch, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Slice builder.  Replaces OneSliceBuilder(scatFac, nElems, n1, n2, d1, d2) and
+ * MultiSlicesBuilder(scatFac, nElems, nSlices, n1, n2, dz, d1, d2)
+ * (cuda_ext/src/SliceBuilder.cu:12-32, 78-100).  scattering_factors_host:
+ * (n_elems, n1, n2/2+1) float32 in HOST memory, the half-spectrum layout of
+ * slice_builder_base.py:30-33; it is copied (the reference borrows a device buffer).
+ * n_slices = 1 gives the one-slice builder.  symmetric_bandlimit != 0 applies the
+ * circular band-limit of make_one_slice / make_multi_slices(symmetric_bandlimit=True)
+ * (slice_builder_numpy.py:18-26, 37-44).
+ * ------------------------------------------------------------------------------- */
+int emsim_gb300_slice_plan_create(const float* scattering_factors_host, int n_elems, int n_slices, int n1,
+                                  int n2, double dz, double d1, double d2, int symmetric_bandlimit,
+                                  emsim_gb300_slice_plan** plan);
+int emsim_gb300_slice_plan_destroy(emsim_gb300_slice_plan* plan);
+
+/* Histogram of atoms per element (SliceBuilder_kernel.cu:9-61 one slice, 64-123 multi).
+ * coords: (n_atoms, 3) float32 device, columns (z, x, y), rows grouped by element in
+ * the order of elem_counts; elem_counts: (n_elems,) uint32 device.  out: float32
+ * (n_elems, n1, n2) resp. (n_elems, n_slices, n1, n2); fully written (no pre-zeroing
+ * needed).  Counts are exact integers and independent of execution order. */
+int emsim_gb300_bin_atoms_one_slice(emsim_gb300_slice_plan* plan, const float* coords, unsigned n_atoms,
+                                    const uint32_t* elem_counts, float* out, void* stream);
+int emsim_gb300_bin_atoms_multi_slices(emsim_gb300_slice_plan* plan, const float* coords, unsigned n_atoms,
+                                       const uint32_t* elem_counts, float* out, void* stream);
+
+/* Bytes of device workspace emsim_gb300_make_slices needs for this plan. */
+size_t emsim_gb300_make_slices_workspace_size(const emsim_gb300_slice_plan* plan);
+
+/* Projected-potential slices from histograms (SliceBuilder.cu:39-64, 108-133 plus the
+ * band-limit of slice_builder_cuda.py:88-99 and the clip at 1e-13).
+ * hist: (n_elems, n_slices, n1, n2) float32 device; out: (n_slices, n1, n2) float32.
+ * workspace: device buffer of at least emsim_gb300_make_slices_workspace_size bytes,
+ * 256-byte aligned. */
+int emsim_gb300_make_slices(emsim_gb300_slice_plan* plan, const float* hist, float* out, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EMSIM_GB300_H */

@@ -1,0 +1,166 @@
+"""Host-side logic of the product package, on CPU: front-end geometry, physics and
+scattering factors against the reference goldens, the algebra behind the fused slice
+build, backend registration and the C ABI's exported symbols."""
+import ctypes
+import re
+import types
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from emsim_gb300 import _native, atoms, config, elem, physics
+from oracle import multislice as om
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_physics_matches_golden(golden):
+    g = golden("physics")
+    np.testing.assert_array_equal([physics.electron_wave_length_angstrom(k) for k in g["kev"]], g["wave_length"])
+    np.testing.assert_array_equal([physics.electron_relativity_gamma(k) for k in g["kev"]], g["gamma"])
+    np.testing.assert_array_equal([physics.interaction_parameter(k) for k in g["kev"]], g["sigma"])
+    for kev, cs, df, ap in g["scherzer"]:
+        assert physics.scherzer_condition(physics.electron_wave_length_angstrom(kev), cs) == (df, ap)
+
+
+@pytest.mark.parametrize("tag", ["a", "b", "c"])
+def test_scattering_factors_match_golden(golden, tag):
+    g = golden("scattering")
+    n1, n2, d1, d2 = g[f"grid_{tag}"]
+    np.testing.assert_array_equal(elem.scattering_factors2d(list(g["zs"]), int(n1), int(n2), d1, d2),
+                                  g[f"sf2d_{tag}"])
+    np.testing.assert_array_equal(elem.scattering_factors_half(list(g["zs"]), int(n1), int(n2), d1, d2),
+                                  g[f"half_{tag}"])
+
+
+def test_front_end_geometry_matches_oracle(golden):
+    g = golden("pipe")
+    mol = atoms.AtomList(g["blob_elements"], g["blob_coords"])
+    c = atoms.centralize(mol)
+    np.testing.assert_array_equal(c.coordinates, om.centralize(g["blob_coords"]))
+    s, uz, cnt = atoms.sort_elements_and_count(c, [1, 8])
+    _, xyz, uz2, cnt2 = om.sort_elements_and_count(g["blob_elements"], c.coordinates, [1, 8])
+    np.testing.assert_array_equal(uz, uz2)
+    np.testing.assert_array_equal(cnt, cnt2)
+    assert 1 in uz and cnt[list(uz).index(1)] == 0
+    assert atoms.determine_box_size(tuple(s.space), (2.0, 1.0, 1.0), (None, 32, 32)) == \
+        om.finalize_slice_size(s.space, (1.0, 1.0), 2.0, 32, None)
+    # flat axes become 3 A thick
+    assert atoms.determine_box_size((0.0, 10.0, 10.0), (2.0, 1.0, 1.0), (None, None, None)) == (2, 10, 10)
+
+
+def test_rotation_matches_reference_convention():
+    q = np.array([0.5, 0.5, 0.5, 0.5])
+    np.testing.assert_allclose(atoms.get_rotation_mattrices(q)[0], om.rotation_matrix(q))
+    r = atoms.get_rotation_mattrices(atoms.random_uniform_quaternions(5, np.random.default_rng(0)))
+    np.testing.assert_allclose(r @ r.transpose(0, 2, 1), np.broadcast_to(np.eye(3), (5, 3, 3)), atol=1e-12)
+
+
+def _bandlimit_full(n1, n2):
+    """Python restatement of the engine's full-spectrum band-limit (slices.cu)."""
+    r = min(n1, n2) // 2
+
+    def centred(i, n):
+        return ((i + n // 2) % n) + (-n // 2)
+
+    h2 = n2 // 2
+
+    def G(i, j):
+        if j > h2:
+            return 0.0
+        fil = 1.0 if centred(i, n1) ** 2 + centred(j, n2) ** 2 <= r * r else 0.0
+        selfc = j == 0 or (n2 % 2 == 0 and j == h2)
+        return (1.0 if selfc else 2.0) * fil
+
+    F = np.empty((n1, n2))
+    for i in range(n1):
+        for j in range(n2):
+            F[i, j] = 0.5 * (G(i, j) + G((n1 - i) % n1, (n2 - j) % n2))
+    return F
+
+
+@pytest.mark.parametrize("n1,n2", [(16, 16), (15, 15), (12, 20), (9, 14)])
+def test_bandlimit_as_full_spectrum_filter(n1, n2):
+    """irfft2(rfft2(V) * fil_half) == Re ifft2(F * fft2(V)) with the symmetrised F, also
+    for odd sizes where numpy's centred grid makes fil asymmetric."""
+    rng = np.random.default_rng(n1 * 100 + n2)
+    v = rng.normal(size=(n1, n2))
+    ref = np.fft.irfft2(np.fft.rfft2(v) * om.bandlimit_mask_half(n1, n2), s=(n1, n2))
+    F = _bandlimit_full(n1, n2)
+    np.testing.assert_array_equal(F, F[(-np.arange(n1)) % n1][:, (-np.arange(n2)) % n2])
+    got = np.fft.ifft2(F * np.fft.fft2(v))
+    assert np.abs(got.imag).max() < 1e-12
+    np.testing.assert_allclose(got.real, ref, atol=1e-12)
+
+
+def test_packed_pair_slice_build():
+    """V_a + i V_b = ifft2(sum_e T_e fft2(h_ea + i h_eb)) for real symmetric T_e: two
+    slices per complex transform, as the engine builds them."""
+    rng = np.random.default_rng(5)
+    n1 = n2 = 16
+    sf = om.scattering_factors_half([6, 8], n1, n2, 0.5, 0.5)
+    hist = rng.poisson(0.3, size=(2, 2, n1, n2)).astype(np.float64)
+    ref = om.make_slices(hist, sf, "fftw", np.float64)
+    F = _bandlimit_full(n1, n2)
+    h = n2 // 2 + 1
+    full = np.empty((2, n1, n2))
+    for e in range(2):
+        for i in range(n1):
+            for j in range(n2):
+                full[e, i, j] = sf[e, i, j] if j < h else sf[e, (n1 - i) % n1, n2 - j]
+    T = F[None] * full / (n1 * n2)
+    z = hist[:, 0] + 1j * hist[:, 1]
+    w = np.fft.ifft2((T * np.fft.fft2(z)).sum(axis=0)) * (n1 * n2)
+    np.testing.assert_allclose(np.maximum(w.real, 1e-13), ref[0], atol=1e-12)
+    np.testing.assert_allclose(np.maximum(w.imag, 1e-13), ref[1], atol=1e-12)
+
+
+def test_register_with_emsim_config():
+    calls = []
+    cfg = types.SimpleNamespace(_current_backend="numpy-backend", set_backend=lambda b="numpy": calls.append(b))
+    fake = types.SimpleNamespace(config=cfg)
+    config.register(fake)
+    config.register(fake)  # idempotent
+    cfg.set_backend("gb300")
+    assert isinstance(cfg._current_backend, config.Gb300Backend)
+    cfg.set_backend("fftw")
+    assert calls == ["fftw"]
+
+
+# ---------------------------------------------------------------------------------
+# C ABI
+# ---------------------------------------------------------------------------------
+def _declared_symbols():
+    text = (ROOT / "include" / "emsim_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(emsim_gb300_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_capi_exports_every_declared_symbol():
+    lib = _native.load()
+    declared = _declared_symbols()
+    assert len(declared) >= 15
+    for name in declared:
+        assert hasattr(lib, name), name
+        assert name in _native.SIGNATURES, f"{name} missing from the ctypes signatures"
+    assert set(_native.SIGNATURES) == set(declared)
+    assert lib.emsim_gb300_abi_version() == 1
+
+
+def test_capi_rejects_bad_arguments_without_gpu():
+    lib = _native.load()
+    h = ctypes.c_void_p()
+    assert lib.emsim_gb300_wave_plan_create(0, 8, 1.0, 1.0, 0.025, 1.4, ctypes.byref(h)) == 1
+    assert "positive" in _native.last_error()
+    assert lib.emsim_gb300_wave_plan_create(8, 8, -1.0, 1.0, 0.025, 1.4, ctypes.byref(h)) == 1
+    assert lib.emsim_gb300_slice_plan_create(None, 1, 1, 8, 8, 1.0, 1.0, 1.0, 1, ctypes.byref(h)) == 1
+    assert lib.emsim_gb300_intensity(None, None, 4, None) == 1
+    assert lib.emsim_gb300_make_slices_workspace_size(None) == 0
+    with pytest.raises(_native.NativeError):
+        _native.call("emsim_gb300_init_wave", None, 1.0, None, 1, None)
+
+
+def test_native_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(_native.NativeUnavailable):
+        _native.load(tmp_path / "nope.so")
