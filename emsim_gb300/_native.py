@@ -20,6 +20,7 @@ _pp = ctypes.POINTER(ctypes.c_void_p)
 SIGNATURES = {
     "emsim_gb300_abi_version": (_c_int, []),
     "emsim_gb300_last_error": (ctypes.c_char_p, []),
+    "emsim_gb300_check_device_error": (_c_int, [ctypes.POINTER(ctypes.c_int)]),
     "emsim_gb300_wave_plan_create": (_c_int, [_c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _pp]),
     "emsim_gb300_wave_plan_destroy": (_c_int, [_c_vp]),
     "emsim_gb300_init_wave": (_c_int, [_c_vp, _c_dbl, _c_vp, _c_int, _c_vp]),
@@ -93,3 +94,10 @@ def call(name: str, *args) -> None:
 
 def last_error() -> str:
     return load().emsim_gb300_last_error().decode(errors="replace")
+
+
+def check_device_error() -> int:
+    """Synchronise and read (and clear) the device error word; 0 = no kernel gave up."""
+    code = ctypes.c_int(0)
+    call("emsim_gb300_check_device_error", ctypes.byref(code))
+    return code.value

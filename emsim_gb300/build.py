@@ -21,8 +21,10 @@ INCLUDE = PKG.parent / "include"
 LIB_DIR = PKG / "_lib"
 LIB = LIB_DIR / "libemsim_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-diag-suppress", "177"]
+# host code keeps the reference's float32 evaluation order: no fused multiply-add
+# contraction (GCC contracts by default on aarch64)
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr", "-diag-suppress", "177"]
 
 
 def nvcc() -> str:

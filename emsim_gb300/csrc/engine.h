@@ -33,7 +33,8 @@ struct RowArgs {
     float sigma = 0.f;
     float2 const_val = {0.f, 0.f};
     int n_rows = 0;
-    const float2* tw = nullptr;  // FFT twiddle table of the device (twiddle_table())
+    const float2* tw = nullptr;  // per-pass twiddle tables of the device (twiddle_table())
+    int* err = nullptr;          // device error word (error_word())
 };
 
 // ---------------------------------------------------------------------------
@@ -47,13 +48,15 @@ enum ColMode : int {
 };
 
 struct ColArgs {
-    const float2* tw = nullptr;  // FFT twiddle table of the device (twiddle_table())
+    const float2* tw = nullptr;  // per-pass twiddle tables of the device (twiddle_table())
+    int* err = nullptr;          // device error word (error_word())
     float2* data = nullptr;
     long long img_stride = 0;
     int n_rows = 0;  // FFT length along columns (n1)
     int n_cols = 0;  // n2
-    // propagate: separable FP64-derived factors p1[k1] (1/N folded in), p2[k2]
-    const float2* p1 = nullptr;
+    // propagate: separable FP64-derived factors p1[k1] (1/N folded in; .z holds the
+    // band-limit cutoff |k2| <= cut of row k1 as int bits), p2[k2]
+    const float4* p1 = nullptr;
     const float2* p2 = nullptr;
     float dfx = 0.f, dfy = 0.f;  // reference float32 frequency steps
     float filter2 = 0.f;         // (0.6667 * fmax)^2 in float32
@@ -87,6 +90,8 @@ int generic_dft_cols(float2* data, int n_rows, int n_cols, bool inverse, const f
 int ensure_twiddles(int device);
 // device address of the FFT twiddle table on the current device (after ensure_twiddles)
 const float2* twiddle_table();
+// device address of the error word kernels set when a bounded wait gives up
+int* error_word();
 
 // opt a kernel into more than 48 KB of dynamic shared memory (once per device)
 int ensure_smem_attr(const void* func, size_t smem_bytes);
@@ -98,7 +103,10 @@ int ew_fill(float2* out, long long n, float2 value, cudaStream_t st);
 int ew_intensity(const float2* in, float* out, long long n, cudaStream_t st);
 int ew_propagate(float2* data, const ColArgs& a, int n_img, cudaStream_t st);
 int ew_lens(float2* data, const ColArgs& a, int n_img, cudaStream_t st);
-int prop_tables(float2* p1, float2* p2, int n1, int n2, double dfx64, double dfy64, double phase_coef,
-                double inv_n, cudaStream_t st);
+int prop_tables(float4* p1, float2* p2, const int* cut, int n1, int n2, double dfx64, double dfy64,
+                double phase_coef, double inv_n, cudaStream_t st);
+// band-limit cutoffs: cut[k1] = largest |k2| with f2(k1, k2) <= filter2 in the reference's
+// float32 arithmetic (f2 grows with |k2|), -1 when even k2 = 0 is cut
+void bandlimit_cutoffs(int n1, int n2, float dfx, float dfy, float filter2, int* cut);
 
 }  // namespace emsim_gb300

@@ -13,8 +13,8 @@
 // radix-R pass lets thread t run the 8/R butterflies j = t + q*T, whose inputs are the
 // same eight positions, so every pass (first, middle or last) starts from that layout
 // and the first gather / last scatter never touch shared memory.  Only the passes in
-// between exchange through shared memory, with one padding slot every 8 elements so
-// the stride-8 scatter of the first pass is free of bank conflicts.
+// between exchange through shared memory, laid out so that the passes' scatters and
+// gathers are free of bank conflicts (see RowLayout / ColLayout).
 //
 // Two shared-memory layouts:
 //   RowLayout: each sequence owns a contiguous padded region; threads of a sequence are
@@ -32,14 +32,17 @@ constexpr int TW_LOG2 = 12;
 constexpr int TW_SIZE = 1 << TW_LOG2;  // largest fast-path length
 constexpr float SQRT1_2 = 0.70710678118654752440f;
 
-// The twiddle table tw[m] = exp(-2 pi i m / TW_SIZE), m < TW_SIZE, lives in device memory
-// (filled once per device from FP64 sincospi) and is passed to the kernels by address.
 
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
 
-template <bool INV>
+// The device twiddle table holds exp(-2 pi i m / TW_SIZE), m < TW_SIZE (FP64-derived);
+// W_L^q of any power-of-two L <= TW_SIZE is entry q * TW_SIZE / L.
+
+// Twiddle tables are read-only and never alias the exchange buffer; TW_SMEM selects a
+// shared-memory copy (plain load) or the device table (read-only cache).
+template <bool INV, bool TW_SMEM>
 __device__ __forceinline__ float2 twiddle(const float2* __restrict__ tw, int m) {
-    float2 w = __ldg(tw + m);
+    const float2 w = TW_SMEM ? tw[m] : __ldg(tw + m);
     return INV ? make_float2(w.x, -w.y) : w;
 }
 
@@ -87,10 +90,19 @@ __device__ __forceinline__ void dft8(float2& y0, float2& y1, float2& y2, float2&
     y7 = csub(e3, o3);
 }
 
+// Row layout: sequence b owns N consecutive float2 slots; element p sits at slot
+// p ^ G(p >> 4) with G(h) = (h & 7) | ((h & 4) << 1).  The XOR permutes slots inside each
+// 16-slot (128-byte) block, so for 16 consecutive threads (T >= 16) every access of the
+// passes is conflict-free: contiguous gathers t + m*T (constant XOR), the stride-8
+// scatter of the Ns = 1 pass (t/2 spreads the low bits), and the Ns = 8 scatter (bit 2
+// of p >> 4 moves the two 8-thread groups into different halves of the block).
 template <int N>
 struct RowLayout {
-    static constexpr int STRIDE = N + N / 8;  // float2 per sequence incl. padding
-    __device__ __forceinline__ static int addr(int b, int p) { return b * STRIDE + p + (p >> 3); }
+    static constexpr int STRIDE = N;
+    __device__ __forceinline__ static int addr(int b, int p) {
+        const int h = p >> 4;
+        return b * STRIDE + (p ^ ((h & 7) | ((h & 4) << 1)));
+    }
     static constexpr int words(int B) { return B * STRIDE; }
 };
 
@@ -111,9 +123,9 @@ __device__ __forceinline__ void tile_sync() {
 // One radix-R Stockham pass over the register-held values.
 // If LAST, the outputs stay in registers (slot m = q + r*(8/R) holds position t + m*T);
 // otherwise they are scattered to shared memory.
-template <int N, int R, bool INV, bool LAST, class AddrF>
-__device__ __forceinline__ void stockham_pass(float2 (&v)[8], int Ns, float2* sm, int b, int t, AddrF addr,
-                                              const float2* __restrict__ tw) {
+template <int N, int R, bool INV, bool LAST, bool TW_SMEM, class AddrF>
+__device__ __forceinline__ void stockham_pass(float2 (&v)[8], int Ns, float2* __restrict__ sm, int b, int t,
+                                              AddrF addr, const float2* __restrict__ ptw) {
     constexpr int T = N / 8;
     constexpr int Q = 8 / R;  // butterflies per thread
 #pragma unroll
@@ -124,10 +136,23 @@ __device__ __forceinline__ void stockham_pass(float2 (&v)[8], int Ns, float2* sm
 #pragma unroll
         for (int r = 0; r < R; ++r) x[r] = v[q + r * Q];
         if (Ns > 1) {
-            // W_{Ns R}^{r k} = W_TW^{r k TW/(Ns R)}
-            const int step = TW_SIZE / (Ns * R);
-#pragma unroll
-            for (int r = 1; r < R; ++r) x[r] = cmul(x[r], twiddle<INV>(tw, r * k * step));
+            // W_{Ns R}^{r k}: one table load of w = W_{Ns R}^k, higher powers by complex
+            // products (at most three roundings deep, ~3e-7 relative)
+            const float2 w1 = twiddle<INV, TW_SMEM>(ptw, k * (TW_SIZE / (Ns * R)));
+            x[1] = cmul(x[1], w1);
+            if (R >= 4) {
+                const float2 w2 = cmul(w1, w1);
+                const float2 w3 = cmul(w2, w1);
+                x[2] = cmul(x[2], w2);
+                x[3] = cmul(x[3], w3);
+                if (R == 8) {
+                    const float2 w4 = cmul(w2, w2);
+                    x[4] = cmul(x[4], w4);
+                    x[5] = cmul(x[5], cmul(w4, w1));
+                    x[6] = cmul(x[6], cmul(w4, w2));
+                    x[7] = cmul(x[7], cmul(w4, w3));
+                }
+            }
         }
         if (R == 8) dft8<INV>(x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7]);
         else if (R == 4) dft4<INV>(x[0], x[1], x[2], x[3]);
@@ -146,9 +171,10 @@ __device__ __forceinline__ void stockham_pass(float2 (&v)[8], int Ns, float2* sm
 // Full length-N transform of the register-held sequence (see the register contract).
 // All threads of the tile must call this together.  Shared memory is free again on
 // return.  Unnormalised in both directions.
-template <int N, bool INV, bool WARP_ONLY, class AddrF>
-__device__ __forceinline__ void fft_regs(float2 (&v)[8], float2* sm, int b, int t, AddrF addr,
-                                         const float2* __restrict__ tw) {
+// ptw: the twiddle table (shared-memory copy when TW_SMEM, else device memory).
+template <int N, bool INV, bool WARP_ONLY, bool TW_SMEM = false, class AddrF>
+__device__ __forceinline__ void fft_regs(float2 (&v)[8], float2* __restrict__ sm, int b, int t, AddrF addr,
+                                         const float2* __restrict__ ptw) {
     static_assert(N >= 8 && N <= TW_SIZE && (N & (N - 1)) == 0, "power-of-two length 8..4096");
     constexpr int T = N / 8;
     constexpr int LOG = ilog2(N);
@@ -165,13 +191,13 @@ __device__ __forceinline__ void fft_regs(float2 (&v)[8], float2* sm, int b, int 
         }
         const bool last = (p == NPASS - 1);
         if (p < N8) {
-            if (last) stockham_pass<N, 8, INV, true>(v, Ns, sm, b, t, addr, tw);
-            else stockham_pass<N, 8, INV, false>(v, Ns, sm, b, t, addr, tw);
+            if (last) stockham_pass<N, 8, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, ptw);
+            else stockham_pass<N, 8, INV, false, TW_SMEM>(v, Ns, sm, b, t, addr, ptw);
             Ns *= 8;
         } else if (REM == 2) {
-            stockham_pass<N, 4, INV, true>(v, Ns, sm, b, t, addr, tw);
+            stockham_pass<N, 4, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, ptw);
         } else {
-            stockham_pass<N, 2, INV, true>(v, Ns, sm, b, t, addr, tw);
+            stockham_pass<N, 2, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, ptw);
         }
         if (!last) tile_sync<WARP_ONLY>();
     }

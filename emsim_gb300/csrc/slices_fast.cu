@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(512) slice_rows_fwd_kernel(SliceArgs a) {
 }
 
 template <int N>
-__global__ void __launch_bounds__(ColThreads<N>::MAX) slice_cols_kernel(SliceArgs a) {
+__global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS) slice_cols_kernel(SliceArgs a) {
     constexpr int T = N / 8;
     extern __shared__ float2 sm[];
     const int B = blockDim.x / T;

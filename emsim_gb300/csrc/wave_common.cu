@@ -4,12 +4,21 @@
 #include <set>
 #include <utility>
 
-#include "wave_passes.cuh"
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include <cudaTypedefs.h>
+
+#include "wave_tma.cuh"
 
 namespace emsim_gb300 {
 
 // exp(-2 pi i m / TW_SIZE); one copy per device, written once by init_twiddle_kernel
 static __device__ float2 g_twiddle[fft::TW_SIZE];
+// error word: kernels record tma::DEV_MBAR_TIMEOUT here when a bounded wait gives up
+static __device__ int g_dev_error;
 
 // ---------------------------------------------------------------------------------
 // error string (per host thread)
@@ -33,6 +42,7 @@ __global__ void init_twiddle_kernel() {
 static std::mutex g_init_mu;
 static std::set<int> g_twiddle_ready;
 static const float2* g_twiddle_addr[64] = {};
+static int* g_error_addr[64] = {};
 static std::set<std::pair<int, const void*>> g_smem_ready;
 
 // The table is written by a kernel on the legacy default stream and waited for, so it is
@@ -47,6 +57,9 @@ int ensure_twiddles(int device) {
     void* addr = nullptr;
     EMSIM_CHECK_CUDA(cudaGetSymbolAddress(&addr, g_twiddle));
     g_twiddle_addr[device] = (const float2*)addr;
+    void* eaddr = nullptr;
+    EMSIM_CHECK_CUDA(cudaGetSymbolAddress(&eaddr, g_dev_error));
+    g_error_addr[device] = (int*)eaddr;
     g_twiddle_ready.insert(device);
     return EMSIM_GB300_OK;
 }
@@ -55,6 +68,76 @@ const float2* twiddle_table() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
     return g_twiddle_addr[dev];
+}
+
+int* error_word() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    return g_error_addr[dev];
+}
+
+// ---------------------------------------------------------------------------------
+// TMA support: persistent grid sizing and tensor maps
+// ---------------------------------------------------------------------------------
+bool tma_enabled() {
+    static const bool on = [] {
+        const char* v = std::getenv("EMSIM_GB300_PASSES");
+        return !(v && std::strcmp(v, "simple") == 0);
+    }();
+    return on;
+}
+
+static std::map<std::tuple<int, const void*, int, size_t>, int> g_occ;
+
+int persistent_grid(const void* func, int threads, size_t smem, int n_tiles) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int per_sm = 0, n_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_init_mu);
+        auto key = std::make_tuple(dev, func, threads, smem);
+        auto it = g_occ.find(key);
+        if (it != g_occ.end()) {
+            per_sm = it->second;
+        } else {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, threads, smem) != cudaSuccess ||
+                per_sm < 1)
+                per_sm = 1;
+            g_occ[key] = per_sm;
+        }
+    }
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    long long g = (long long)per_sm * (n_sm > 0 ? n_sm : 1);
+    if (g > n_tiles) g = n_tiles;
+    return g < 1 ? 1 : (int)g;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+int make_col_tensor_map(CUtensorMap* map, const float2* data, long long n_rows_total, int n_cols, int box_cols,
+                        int box_rows) {
+    auto enc = tensor_map_encoder();
+    EMSIM_REQUIRE(enc != nullptr, EMSIM_GB300_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)2 * n_cols, (cuuint64_t)n_rows_total};
+    cuuint64_t strides[1] = {(cuuint64_t)n_cols * sizeof(float2)};
+    cuuint32_t box[2] = {(cuuint32_t)(2 * box_cols), (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(data), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    EMSIM_REQUIRE(r == CUDA_SUCCESS, EMSIM_GB300_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    return EMSIM_GB300_OK;
 }
 
 int ensure_smem_attr(const void* func, size_t smem_bytes) {
@@ -75,11 +158,25 @@ int ensure_smem_attr(const void* func, size_t smem_bytes) {
 #define EMSIM_FAST_SIZES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 #define EMSIM_DECL(N)                                                                  \
     extern template int launch_row_n<N>(int, const RowArgs&, int, cudaStream_t);       \
-    extern template int launch_col_n<N>(int, const ColArgs&, int, cudaStream_t);
+    extern template int launch_col_n<N>(int, const ColArgs&, int, cudaStream_t);       \
+    extern template int launch_row_tma_n<N>(int, const RowArgs&, int, cudaStream_t);   \
+    extern template int launch_col_tma_n<N>(int, const ColArgs&, int, cudaStream_t);
 EMSIM_FAST_SIZES(EMSIM_DECL)
 #undef EMSIM_DECL
 
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
 int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
+    const bool tma = tma_enabled() && n2 >= 16 && ((ops & ROW_CONST_IN) || aligned16(a.in)) &&
+                     (!(ops & ROW_TRANSMIT) || (aligned16(a.slice) && (a.slice_img_stride & 3) == 0));
+    if (tma) {
+        switch (n2) {
+#define EMSIM_CASE(N) \
+    case N: return launch_row_tma_n<N>(ops, a, n_img, st);
+            EMSIM_FAST_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
+        }
+    }
     switch (n2) {
 #define EMSIM_CASE(N) \
     case N: return launch_row_n<N>(ops, a, n_img, st);
@@ -91,6 +188,15 @@ int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
 }
 
 int launch_col(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st) {
+    const bool tma = tma_enabled() && n1 >= 16 && col_tma_B(n1, a.n_cols) >= 2 && aligned16(a.data);
+    if (tma) {
+        switch (n1) {
+#define EMSIM_CASE(N) \
+    case N: return launch_col_tma_n<N>(mode, a, n_img, st);
+            EMSIM_FAST_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
+        }
+    }
     switch (n1) {
 #define EMSIM_CASE(N) \
     case N: return launch_col_n<N>(mode, a, n_img, st);
@@ -233,9 +339,10 @@ __global__ void propagate_kernel(float2* data, ColArgs a) {
     const long long img = blockIdx.y;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int r = (int)(i / a.n_cols), c = (int)(i - (long long)r * a.n_cols);
-        const float f2 = freq_sq_ref(fftfreq_int(r, a.n_rows), fftfreq_int(c, a.n_cols), a.dfx, a.dfy);
+        const float4 q = a.p1[r];
         float2* p = data + img * a.img_stride + i;
-        *p = (f2 <= a.filter2) ? cmul(*p, cmul(a.p1[r], a.p2[c])) : make_float2(0.f, 0.f);
+        const bool keep = abs(fftfreq_int(c, a.n_cols)) <= __float_as_int(q.z);
+        *p = keep ? cmul(*p, cmul(make_float2(q.x, q.y), a.p2[c])) : make_float2(0.f, 0.f);
     }
 }
 
@@ -268,10 +375,11 @@ int ew_lens(float2* data, const ColArgs& a, int n_img, cudaStream_t st) {
     return EMSIM_GB300_OK;
 }
 
-// p1[k1] = exp(-i phase_coef fx^2) * inv_n, p2[k2] = exp(-i phase_coef fy^2);
-// phase_coef = pi * lambda * dz.  The phase is formed and reduced mod 2 pi in FP64.
-__global__ void prop_table_kernel(float2* p1, float2* p2, int n1, int n2, double dfx64, double dfy64,
-                                  double phase_coef, double inv_n) {
+// p1[k1] = {exp(-i phase_coef fx^2) * inv_n, band-limit cutoff of row k1}, p2[k2] =
+// exp(-i phase_coef fy^2); phase_coef = pi * lambda * dz.  The phase is formed and reduced
+// mod 2 pi in FP64.
+__global__ void prop_table_kernel(float4* p1, float2* p2, const int* cut, int n1, int n2, double dfx64,
+                                  double dfy64, double phase_coef, double inv_n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n1 + n2) {
         const bool first = i < n1;
@@ -281,16 +389,19 @@ __global__ void prop_table_kernel(float2* p1, float2* p2, int n1, int n2, double
         ph = fma(-TWO_PI, rint(ph * INV_TWO_PI), ph);
         float s, c;
         sincosf((float)ph, &s, &c);
-        const float sc = first ? (float)inv_n : 1.f;
-        const float2 v = make_float2(c * sc, -s * sc);
-        if (first) p1[i] = v;
-        else p2[i - n1] = v;
+        if (first) {
+            const float sc = (float)inv_n;
+            p1[i] = make_float4(c * sc, -s * sc, __int_as_float(cut[i]), 0.f);
+        } else {
+            p2[i - n1] = make_float2(c, -s);
+        }
     }
 }
 
-int prop_tables(float2* p1, float2* p2, int n1, int n2, double dfx64, double dfy64, double phase_coef,
-                double inv_n, cudaStream_t st) {
-    prop_table_kernel<<<ceil_div(n1 + n2, 256), 256, 0, st>>>(p1, p2, n1, n2, dfx64, dfy64, phase_coef, inv_n);
+int prop_tables(float4* p1, float2* p2, const int* cut, int n1, int n2, double dfx64, double dfy64,
+                double phase_coef, double inv_n, cudaStream_t st) {
+    prop_table_kernel<<<ceil_div(n1 + n2, 256), 256, 0, st>>>(p1, p2, cut, n1, n2, dfx64, dfy64, phase_coef,
+                                                              inv_n);
     EMSIM_CHECK_LAUNCH();
     return EMSIM_GB300_OK;
 }
@@ -298,4 +409,18 @@ int prop_tables(float2* p1, float2* p2, int n1, int n2, double dfx64, double dfy
 }  // namespace emsim_gb300
 
 extern "C" const char* emsim_gb300_last_error(void) { return emsim_gb300::get_error(); }
+
+extern "C" int emsim_gb300_check_device_error(int* code) {
+    using namespace emsim_gb300;
+    EMSIM_REQUIRE(code != nullptr, EMSIM_GB300_ERR_INVALID, "check_device_error: null output");
+    *code = 0;
+    int dev = 0;
+    EMSIM_CHECK_CUDA(cudaGetDevice(&dev));
+    EMSIM_TRY(ensure_twiddles(dev));
+    EMSIM_CHECK_CUDA(cudaDeviceSynchronize());
+    int zero = 0;
+    EMSIM_CHECK_CUDA(cudaMemcpyFromSymbol(code, g_dev_error, sizeof(int)));
+    EMSIM_CHECK_CUDA(cudaMemcpyToSymbol(g_dev_error, &zero, sizeof(int)));
+    return EMSIM_GB300_OK;
+}
 extern "C" int emsim_gb300_abi_version(void) { return EMSIM_GB300_ABI_VERSION; }

@@ -1,8 +1,10 @@
 // Explicit instantiations of the fused row/column passes for length(s): 1024.
 // One translation unit per size group so the fast path compiles in parallel.
-#include "wave_passes.cuh"
+#include "wave_tma.cuh"
 
 namespace emsim_gb300 {
 template int launch_row_n<1024>(int, const RowArgs&, int, cudaStream_t);
 template int launch_col_n<1024>(int, const ColArgs&, int, cudaStream_t);
+template int launch_row_tma_n<1024>(int, const RowArgs&, int, cudaStream_t);
+template int launch_col_tma_n<1024>(int, const ColArgs&, int, cudaStream_t);
 }  // namespace emsim_gb300

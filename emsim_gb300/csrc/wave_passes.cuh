@@ -92,14 +92,29 @@ __device__ __forceinline__ float2 lens_factor(int k1, int k2, double fy2, double
     return make_float2(c * a.lens_scale, -s * a.lens_scale);
 }
 
-// threads per CTA of the column pass: up to 512 (128 registers), 1024 from length 2048 on
+// threads per CTA of the column pass: 512 with two CTAs per SM (64 registers), 1024 from
+// length 2048 on
 template <int N>
 struct ColThreads {
     static constexpr int MAX = (N / 8 >= 256) ? 1024 : 512;
+    static constexpr int MIN_BLOCKS = (N / 8 >= 256) ? 1 : 2;
 };
 
+// x P(k1, k2) / N inside the band-limit disc, 0 outside, for column `col`, rows t + m*T
+template <int N>
+__device__ __forceinline__ void propagate_col(float2 (&v)[8], int col, int t, const ColArgs& a) {
+    constexpr int T = N / 8;
+    const int k2a = abs(fftfreq_int(col, a.n_cols));
+    const float2 p2 = __ldg(a.p2 + col);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const float4 q = __ldg(a.p1 + t + m * T);
+        v[m] = (k2a <= __float_as_int(q.z)) ? cmul(v[m], cmul(make_float2(q.x, q.y), p2)) : make_float2(0.f, 0.f);
+    }
+}
+
 template <int N, int MODE>
-__global__ void __launch_bounds__(ColThreads<N>::MAX) col_pass_kernel(ColArgs a) {
+__global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS) col_pass_kernel(ColArgs a) {
     constexpr int T = N / 8;
     extern __shared__ float2 sm[];
     const int B = blockDim.x / T;
@@ -117,17 +132,7 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX) col_pass_kernel(ColArgs a)
 
     if (MODE != COL_INV) fft::fft_regs<N, false, false>(v, sm, b, t, addr, a.tw);
 
-    if (MODE == COL_PROPAGATE) {
-        const int k2 = fftfreq_int(col, a.n_cols);
-        const float2 p2 = __ldg(a.p2 + col);
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            const int r = t + m * T;
-            const int k1 = fftfreq_int(r, N);
-            const float f2 = freq_sq_ref(k1, k2, a.dfx, a.dfy);
-            v[m] = (f2 <= a.filter2) ? cmul(v[m], cmul(__ldg(a.p1 + r), p2)) : make_float2(0.f, 0.f);
-        }
-    } else if (MODE == COL_LENS) {
+    if (MODE == COL_PROPAGATE) propagate_col<N>(v, col, t, a); else if (MODE == COL_LENS) {
         const int k2 = fftfreq_int(col, a.n_cols);
         const double fy = (double)k2 * a.dfy64;
         const double fy2 = fy * fy;

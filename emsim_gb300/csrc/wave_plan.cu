@@ -31,14 +31,39 @@ struct emsim_gb300_wave_plan {
     bool fast = false;
     int device = 0;
     const float2* tw = nullptr;  // FFT twiddle table of the plan's device
+    int* err = nullptr;          // device error word of the plan's device
     float2* tw1 = nullptr;  // generic path: exp(-2 pi i m / n1)
     float2* tw2 = nullptr;
-    float2* prop = nullptr;  // PROP_SLOTS x (n1 + n2) propagator factor tables
+    char* prop = nullptr;    // PROP_SLOTS x (float4 p1[n1] + float2 p2[n2]) propagator tables
+    int* cut = nullptr;      // band-limit cutoff per row (bandlimit_cutoffs)
     double prop_dz[PROP_SLOTS];
     int prop_used = 0;
     int prop_next = 0;
     std::mutex mu;
 };
+
+namespace emsim_gb300 {
+
+// Reference mask f2 <= filter2 with f2 = fl(fl(fx^2) + fl(fy^2)), fx = fl(k1 * dfx),
+// evaluated in float32 (this translation unit is compiled with -ffp-contract=off); for
+// fixed k1 it is monotone in |k2|, so one cutoff per row describes the whole disc.
+void bandlimit_cutoffs(int n1, int n2, float dfx, float dfy, float filter2, int* cut) {
+    for (int i = 0; i < n1; ++i) {
+        const float fx = (float)fftfreq_int(i, n1) * dfx;
+        const float fx2 = fx * fx;
+        int c = -1;
+        for (int m = 0; m <= n2 / 2; ++m) {
+            const float fy = (float)m * dfy;
+            const float fy2 = fy * fy;
+            const float f2 = fx2 + fy2;
+            if (f2 <= filter2) c = m;
+            else break;
+        }
+        cut[i] = c;
+    }
+}
+
+}  // namespace emsim_gb300
 
 namespace {
 
@@ -66,30 +91,36 @@ int make_tw(int n, float2** out) {
 // the caller's stream the first time a dz is seen and kept; with more than PROP_SLOTS
 // distinct dz values the oldest slot is rewritten (calls with different dz on different
 // streams of one plan must then be ordered by the caller).
-int get_prop(emsim_gb300_wave_plan* p, double dz, cudaStream_t st, const float2** p1, const float2** p2) {
+size_t prop_slot_bytes(const emsim_gb300_wave_plan* p) {
+    return (size_t)p->n1 * sizeof(float4) + (size_t)p->n2 * sizeof(float2);
+}
+
+int get_prop(emsim_gb300_wave_plan* p, double dz, cudaStream_t st, const float4** p1, const float2** p2) {
     std::lock_guard<std::mutex> lk(p->mu);
-    const int len = p->n1 + p->n2;
+    const size_t sb = prop_slot_bytes(p);
     for (int i = 0; i < p->prop_used; ++i) {
         if (p->prop_dz[i] == dz) {
-            *p1 = p->prop + (size_t)i * len;
-            *p2 = *p1 + p->n1;
+            *p1 = reinterpret_cast<const float4*>(p->prop + (size_t)i * sb);
+            *p2 = reinterpret_cast<const float2*>(*p1 + p->n1);
             return EMSIM_GB300_OK;
         }
     }
     int slot = p->prop_used < PROP_SLOTS ? p->prop_used++ : (p->prop_next++ % PROP_SLOTS);
-    float2* t1 = p->prop + (size_t)slot * len;
+    float4* t1 = reinterpret_cast<float4*>(p->prop + (size_t)slot * sb);
+    float2* t2 = reinterpret_cast<float2*>(t1 + p->n1);
     const double coef = M_PI * p->wave_length * dz;
-    EMSIM_TRY(prop_tables(t1, t1 + p->n1, p->n1, p->n2, p->dfx64, p->dfy64, coef,
+    EMSIM_TRY(prop_tables(t1, t2, p->cut, p->n1, p->n2, p->dfx64, p->dfy64, coef,
                           1.0 / ((double)p->n1 * (double)p->n2), st));
     p->prop_dz[slot] = dz;
     *p1 = t1;
-    *p2 = t1 + p->n1;
+    *p2 = t2;
     return EMSIM_GB300_OK;
 }
 
 ColArgs base_col(const emsim_gb300_wave_plan* p, float2* data) {
     ColArgs a;
     a.tw = p->tw;
+    a.err = p->err;
     a.data = data;
     a.img_stride = (long long)p->n1 * p->n2;
     a.n_rows = p->n1;
@@ -105,6 +136,7 @@ ColArgs base_col(const emsim_gb300_wave_plan* p, float2* data) {
 RowArgs base_row(const emsim_gb300_wave_plan* p) {
     RowArgs a;
     a.tw = p->tw;
+    a.err = p->err;
     const long long npix = (long long)p->n1 * p->n2;
     a.in_img_stride = npix;
     a.out_img_stride = npix;
@@ -140,7 +172,8 @@ int g_fft2(emsim_gb300_wave_plan* p, const float2* in, float2* out, bool inverse
 }
 
 int g_space(emsim_gb300_wave_plan* p, const float2* in, float2* out, double dz, int nb, cudaStream_t st) {
-    const float2 *p1, *p2;
+    const float4* p1;
+    const float2* p2;
     EMSIM_TRY(get_prop(p, dz, st, &p1, &p2));
     EMSIM_TRY(g_fft2(p, in, out, false, nb, st));
     ColArgs a = base_col(p, out);
@@ -198,6 +231,7 @@ int emsim_gb300_wave_plan_create(int n1, int n2, double d1, double d2, double wa
         if (p->tw1) cudaFree(p->tw1);
         if (p->tw2) cudaFree(p->tw2);
         if (p->prop) cudaFree(p->prop);
+        if (p->cut) cudaFree(p->cut);
         delete p;
         return code;
     };
@@ -207,13 +241,23 @@ int emsim_gb300_wave_plan_create(int n1, int n2, double d1, double d2, double wa
     }
     if ((st = ensure_twiddles(p->device)) != EMSIM_GB300_OK) return fail(st);
     p->tw = twiddle_table();
+    p->err = error_word();
     if (!p->fast) {
         if ((st = make_tw(n1, &p->tw1)) != EMSIM_GB300_OK) return fail(st);
         if ((st = make_tw(n2, &p->tw2)) != EMSIM_GB300_OK) return fail(st);
     }
-    if (cudaMalloc((void**)&p->prop, sizeof(float2) * (size_t)PROP_SLOTS * (n1 + n2)) != cudaSuccess) {
+    if (cudaMalloc((void**)&p->prop, prop_slot_bytes(p) * PROP_SLOTS) != cudaSuccess ||
+        cudaMalloc((void**)&p->cut, sizeof(int) * n1) != cudaSuccess) {
         set_error("cudaMalloc of propagator tables failed");
         return fail(EMSIM_GB300_ERR_CUDA);
+    }
+    {
+        std::vector<int> cut(n1);
+        bandlimit_cutoffs(n1, n2, p->dfx, p->dfy, p->filter2, cut.data());
+        if (cudaMemcpy(p->cut, cut.data(), sizeof(int) * n1, cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("upload of band-limit cutoffs failed");
+            return fail(EMSIM_GB300_ERR_CUDA);
+        }
     }
     *plan = p;
     return EMSIM_GB300_OK;
@@ -224,6 +268,7 @@ int emsim_gb300_wave_plan_destroy(emsim_gb300_wave_plan* p) {
     cudaFree(p->tw1);
     cudaFree(p->tw2);
     cudaFree(p->prop);
+    cudaFree(p->cut);
     delete p;
     return EMSIM_GB300_OK;
 }
@@ -252,7 +297,8 @@ int emsim_gb300_space_propagate(emsim_gb300_wave_plan* p, const void* wave, doub
     cudaStream_t st = (cudaStream_t)stream;
     float2* out = (float2*)wave_out;
     if (!p->fast) return g_space(p, (const float2*)wave, out, dz, nb, st);
-    const float2 *p1, *p2;
+    const float4* p1;
+    const float2* p2;
     EMSIM_TRY(get_prop(p, dz, st, &p1, &p2));
     RowArgs r = base_row(p);
     r.in = (const float2*)wave;
@@ -278,7 +324,8 @@ int emsim_gb300_singleslice_propagate(emsim_gb300_wave_plan* p, const void* wave
         EMSIM_TRY(ew_transmit((const float2*)wave, slice, out, npix, p->sigma, nb, npix, slice_stride, npix, st));
         return g_space(p, out, out, dz, nb, st);
     }
-    const float2 *p1, *p2;
+    const float4* p1;
+    const float2* p2;
     EMSIM_TRY(get_prop(p, dz, st, &p1, &p2));
     RowArgs r = base_row(p);
     r.in = (const float2*)wave;
@@ -303,7 +350,8 @@ namespace {
 // from the plane wave const_val instead of reading `in`.
 int fast_steps(emsim_gb300_wave_plan* p, const float2* in, bool const_in, float2 const_val, const float* slices,
                int n_slices, long long slices_stride, double dz, float2* work, int nb, cudaStream_t st) {
-    const float2 *p1, *p2;
+    const float4* p1;
+    const float2* p2;
     EMSIM_TRY(get_prop(p, dz, st, &p1, &p2));
     const long long npix = (long long)p->n1 * p->n2;
     RowArgs r = base_row(p);

@@ -1,0 +1,125 @@
+"""Micro-benchmark of the engine's hot calls on synthetic device-resident data.
+
+Times one C-ABI call (median of --reps, CUDA events on the launching stream, L2
+flushed before each rep) and prints a JSON line.  Also the small, bounded driver for
+ncu captures of single kernels.
+
+  python -m emsim_gb300.kernel_bench --case step  --n 512 --batch 64 --slices 4
+  python -m emsim_gb300.kernel_bench --case slices --n 256 --elements 4 --slices 40
+  python -m emsim_gb300.kernel_bench --case bin   --n 256 --slices 40 --atoms 50000
+
+cases: step (multislice_propagate), space (space_propagate), lens (lens_propagate),
+image (multislice_image: plane wave -> slices -> lens -> |psi|^2), slices
+(make_multi_slices), bin (bin_atoms_multi_slices).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+
+import numpy as np
+import torch
+
+from . import _native, backend
+
+
+def _time(fn, reps: int, flush: torch.Tensor) -> float:
+    ts = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    return float(np.median(ts))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="step", choices=["step", "space", "lens", "image", "slices", "bin"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--slices", type=int, default=4)
+    ap.add_argument("--elements", type=int, default=4)
+    ap.add_argument("--atoms", type=int, default=50000)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=2)
+    args = ap.parse_args(argv)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    torch.manual_seed(0)
+    n, B, S = args.n, args.batch, args.slices
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    st = lambda: ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)  # noqa: E731
+    P = backend._ptr
+    out = {"case": args.case, "n": n}
+    if args.case in ("step", "space", "lens", "image"):
+        wp = backend.WavePropagator(n, n, 0.5, 0.5, 200.0)
+        w = torch.ones((B, n, n), dtype=torch.complex64, device=dev)
+        o = torch.empty_like(w)
+        sl = torch.rand((B, S, n, n), dtype=torch.float32, device=dev)
+        img = torch.empty((B, n, n), dtype=torch.float32, device=dev)
+        df = np.full(B, 700.0)
+        h = wp._plan.handle
+        calls = {
+            "step": lambda: _native.call("emsim_gb300_multislice_propagate", h, P(w), P(sl), S, S * n * n, 2.0, P(o),
+                                         B, st()),
+            "space": lambda: _native.call("emsim_gb300_space_propagate", h, P(w), 2.0, P(o), B, st()),
+            "lens": lambda: _native.call("emsim_gb300_lens_propagate", h, P(w), 1.3, 700.0, 0.01, P(o), B, st()),
+            "image": lambda: _native.call("emsim_gb300_multislice_image", h, P(sl), S, S * n * n, 2.0, 20.0, 1.3,
+                                          df.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), B, 0.01, P(img),
+                                          P(o), None, B, st()),
+        }
+        fn = calls[args.case]
+        for _ in range(args.warmup):
+            fn()
+        t = _time(fn, args.reps, flush)
+        px = B * n * n
+        out.update(batch=B, slices=S, seconds=t)
+        if args.case == "step":
+            steps = S + 0.5
+            out.update(slice_steps_per_s=B * S / t, algo_gbs=20.0 * px * S / t / 1e9,
+                       moved_gbs_two_pass=(36.0 * px * S + 16.0 * px) / t / 1e9, per_step_us=1e6 * t / steps)
+        elif args.case in ("space", "lens"):
+            out.update(algo_gbs=16.0 * px / t / 1e9)
+        else:
+            out.update(images_per_s=B / t)
+    elif args.case == "slices":
+        E = args.elements
+        zs = [6, 7, 8, 16, 1, 29][:E]
+        b = backend.MultiSlicesBuilder(zs, S, n, n, 2.0, 1.0, 1.0)
+        hist = torch.poisson(torch.full((E, S, n, n), 0.05, device=dev))
+        o = torch.empty((S, n, n), dtype=torch.float32, device=dev)
+        nbytes = int(_native.load().emsim_gb300_make_slices_workspace_size(b._plan.handle))
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        fn = lambda: _native.call("emsim_gb300_make_slices", b._plan.handle, P(hist), P(o), P(ws), nbytes,  # noqa
+                                  st())
+        for _ in range(args.warmup):
+            fn()
+        t = _time(fn, args.reps, flush)
+        out.update(elements=E, slices=S, seconds=t, slices_per_s=S / t,
+                   algo_gbs=(4.0 * E + 4.0) * S * n * n / t / 1e9)
+    else:
+        zs = [6, 7, 8, 16]
+        b = backend.MultiSlicesBuilder(zs, S, n, n, 2.0, 1.0, 1.0)
+        rng = np.random.default_rng(0)
+        N = args.atoms
+        xyz = ((rng.random((N, 3)) * 2 - 1) * np.array([S, n / 2, n / 2])).astype(np.float32)
+        cnt = np.array([N // 4, N // 4, N // 4, N - 3 * (N // 4)], dtype=np.int32)
+        c = torch.from_numpy(xyz).to(dev)
+        cn = torch.from_numpy(cnt).to(dev)
+        hist = torch.empty((4, S, n, n), dtype=torch.float32, device=dev)
+        fn = lambda: _native.call("emsim_gb300_bin_atoms_multi_slices", b._plan.handle, P(c), N, P(cn),  # noqa
+                                  P(hist), st())
+        for _ in range(args.warmup):
+            fn()
+        t = _time(fn, args.reps, flush)
+        out.update(atoms=N, slices=S, seconds=t, atoms_per_s=N / t,
+                   algo_gbs=(16.0 * N + 4.0 * hist.numel()) / t / 1e9)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -45,6 +45,12 @@ int emsim_gb300_abi_version(void);
 /* Message of the last failed call on this host thread ("" if none). */
 const char* emsim_gb300_last_error(void);
 
+/* Synchronise the current device, then read and clear its device error word: 0 when
+ * no kernel gave up; 1 when a pipelined kernel's bounded wait for a tile copy timed out
+ * (its results are then invalid).  No reference counterpart: the reference reports
+ * CUDA errors on stderr only (WavePropagator.cu:18-20). */
+int emsim_gb300_check_device_error(int* code);
+
 /* ---------------------------------------------------------------------------------
  * Wave propagator.  Replaces WavePropagator(n1, n2, d1, d2, waveLength,
  * relativityGamma) (cuda_ext/src/WavePropagator.cu:14-21; python side

@@ -210,7 +210,13 @@ def test_five_atoms_512(eng):
     i64 = om.intensity(w64.lens_propagate(e64, 1.3, t.defocus, t.aperture))
     assert om.rel_l2(_np(ew), e64) < TOL
     assert om.rel_l2(img, i64) < TOL
-    assert om.rel_l2(img - img.mean(), i64 - i64.mean()) < 1e-3
+    # the image contrast is ~0.4 % of the mean, so float32 intensities alone carry ~1e-3
+    # rel-L2 on I - mean; the engine must sit at the FP32 restatement's own level
+    w32 = om.WavePropagator(512, 512, pix, pix, 200.0, "fftw", np.float32)
+    s32 = om.make_slices(om.bin_atoms_cuda(xyz_s, cnt, (512, 512), (pix, pix)), sf, "fftw", np.float32)
+    i32 = om.intensity(w32.lens_propagate(w32.slice_transmit(w32.init_wave(20.0), s32), 1.3, t.defocus, t.aperture))
+    floor = om.rel_l2(i32 - i32.mean(), i64 - i64.mean())
+    assert om.rel_l2(img - img.mean(), i64 - i64.mean()) < max(2 * floor, 1e-4)
 
 
 @pytest.mark.parametrize("roi,n_atoms", [(64, 3000), (256, 50000)])
@@ -264,3 +270,47 @@ def test_large_wave_properties(eng):
     bl = _np(wp.space_propagate(w, 0.0))  # band-limit only (P = 1 at dz = 0)
     p = _np(wp.space_propagate(bl, 7.0))
     assert abs(np.linalg.norm(p) / np.linalg.norm(bl) - 1) < 1e-5
+
+
+def test_no_device_error_after_runs(eng):
+    from emsim_gb300 import _native
+    wp = eng.WavePropagator(256, 256, 0.5, 0.5, 200.0)
+    sl = np.random.default_rng(51).random((2, 3, 256, 256)).astype(np.float32)
+    wp.image(sl, 2.0, 20.0, 1.3, [700.0, 800.0], 0.01)
+    assert _native.check_device_error() == 0
+
+
+def test_tma_and_simple_passes_agree(eng, tmp_path):
+    """The persistent TMA-staged passes and the one-tile-per-CTA passes are the same
+    arithmetic; run the simple ones in a child process and compare."""
+    import subprocess
+    import sys
+    rng = np.random.default_rng(52)
+    sl = (rng.random((2, 4, 512, 512)) * 2).astype(np.float32)
+    np.save(tmp_path / "sl.npy", sl)
+    code = ("import numpy as np, sys; sys.path.insert(0, %r)\n"
+            "from emsim_gb300 import backend\n"
+            "wp = backend.WavePropagator(512, 512, 0.5, 0.5, 200.0)\n"
+            "sl = np.load(%r)\n"
+            "img, ew = wp.image(sl, 2.0, 20.0, 1.3, [700.0, 900.0], 0.01, return_exit_wave=True)\n"
+            "np.save(%r, img.get()); np.save(%r, ew.get())\n") % (
+        str(__import__("pathlib").Path(__file__).resolve().parent.parent), str(tmp_path / "sl.npy"),
+        str(tmp_path / "img.npy"), str(tmp_path / "ew.npy"))
+    env = dict(__import__("os").environ, EMSIM_GB300_PASSES="simple")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=300)
+    wp = eng.WavePropagator(512, 512, 0.5, 0.5, 200.0)
+    img, ew = wp.image(sl, 2.0, 20.0, 1.3, [700.0, 900.0], 0.01, return_exit_wave=True)
+    np.testing.assert_array_equal(_np(img), np.load(tmp_path / "img.npy"))
+    np.testing.assert_array_equal(_np(ew), np.load(tmp_path / "ew.npy"))
+
+
+@pytest.mark.parametrize("n", [1024, 2048])
+def test_large_fft_parity(eng, n):
+    """Full-size transforms on the 1024 / 2048 fast paths against the oracle."""
+    rng = np.random.default_rng(n)
+    w = _rand_wave(rng, (n, n))
+    sl = (rng.random((2, n, n)) * 2).astype(np.float32)
+    wp = eng.WavePropagator(n, n, 0.1, 0.1, 300.0)
+    o64 = om.WavePropagator(n, n, 0.1, 0.1, 300.0, "fftw", np.float64)
+    assert om.rel_l2(_np(wp.multislice_propagate(w, sl, 0.5)), o64.multislice_propagate(w, sl, 0.5)) < TOL
+    assert om.rel_l2(_np(wp.lens_propagate(w, 1.0, 500.0, 0.02)), o64.lens_propagate(w, 1.0, 500.0, 0.02)) < TOL
