@@ -95,7 +95,9 @@ class ClockSampler:
 # our arm
 # ---------------------------------------------------------------------------------
 class DeviceBatch:
-    """Device-resident inputs and buffers for B blobs; run() queues one full step."""
+    """Device-resident inputs and buffers for B blobs; run() queues one full step:
+    slices of all blobs straight from their atoms (one call), then plane wave ->
+    multislice -> lens -> |psi|^2 for all blobs (one call)."""
 
     def __init__(self, seeds, torch, backend, atoms, pot):
         W = WORKLOAD
@@ -104,54 +106,49 @@ class DeviceBatch:
         dev = torch.device("cuda", torch.cuda.current_device())
         pix = 0.5 * W["resolution"]
         self.pix = pix
-        self.items = []
-        ns_all = set()
+        geo = []
         for s in seeds:
             el, xyz = blob(s)
             mol = atoms.centralize(atoms.AtomList(el, xyz))
             mol, uz, cnt = atoms.sort_elements_and_count(mol)
             ns, n1, n2 = pot.finalize_slice_size(tuple(mol.space), (pix, pix), W["slice_thickness"], W["roi"], None)
-            ns_all.add(ns)
-            self.items.append((torch.from_numpy(mol.coordinates).to(dev), list(uz),
-                               torch.from_numpy(cnt.astype(np.int32)).to(dev), ns))
-        self.ns = max(ns_all)
+            geo.append((mol.coordinates, tuple(int(z) for z in uz), cnt, ns))
+        keys = {(g[1], g[3]) for g in geo}
+        if len(keys) != 1:
+            raise RuntimeError(f"blobs of one batch need equal elements and slice counts, got {sorted(keys)}")
+        (uz, ns), = keys
+        self.ns = ns
         self.n = W["roi"]
         self.B = len(seeds)
-        # one builder (plan) per distinct (elements, n_slices); slice stacks padded to ns
-        self.builders = {}
-        for c, uz, cnt, ns in self.items:
-            key = (tuple(uz), ns)
-            if key not in self.builders:
-                self.builders[key] = backend.MultiSlicesBuilder(uz, ns, self.n, self.n, W["slice_thickness"], pix, pix)
-        self.hist = {k: torch.empty((len(k[0]), k[1], self.n, self.n), dtype=torch.float32, device=dev)
-                     for k in self.builders}
-        self.slices = torch.zeros((self.B, self.ns, self.n, self.n), dtype=torch.float32, device=dev)
+        self.builder = backend.MultiSlicesBuilder(list(uz), ns, self.n, self.n, W["slice_thickness"], pix, pix)
+        xyz = np.ascontiguousarray(np.concatenate([g[0] for g in geo]))
+        counts = np.stack([g[2] for g in geo]).astype(np.uint32)
+        self.n_atoms = int(xyz.shape[0])
+        self.coords = torch.from_numpy(xyz).to(dev)
+        self.counts = torch.from_numpy(counts.view(np.int32)).to(dev)
+        self.slices = torch.empty((self.B, ns, self.n, self.n), dtype=torch.float32, device=dev)
         self.work = torch.empty((self.B, self.n, self.n), dtype=torch.complex64, device=dev)
         self.img = torch.empty((self.B, self.n, self.n), dtype=torch.float32, device=dev)
-        self.ws = {k: torch.empty(max(256, int(backend._native.load().emsim_gb300_make_slices_workspace_size(
-            b._plan.handle))), dtype=torch.uint8, device=dev) for k, b in self.builders.items()}
+        lib = backend._native.load()
+        self.ws_bytes = int(lib.emsim_gb300_build_slices_workspace_size(self.builder._plan.handle, self.n_atoms,
+                                                                       self.B))
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
         self.wp = backend.WavePropagator(self.n, self.n, pix, pix, W["kev"])
         self.df = np.full(self.B, W["defocus"], dtype=np.float64)
-        if len(ns_all) != 1:
-            raise RuntimeError(f"blobs of one batch need equal slice counts, got {sorted(ns_all)}")
 
     def launches_per_step(self) -> int:
-        per_image = 1 + 3  # binning kernel + three slice-build passes (memset is a driver op)
+        # slices: group scan (2) + bucket + bucket scan (3) + scatter + column pass + row pass
+        slices = 2 + 1 + 3 + 1 + 2
         lens = math.ceil(self.B / 64)
-        return self.B * per_image + 2 * self.ns + lens + 1
+        return slices + 2 * self.ns + lens + 1
 
     def run(self):
         import ctypes
         nat = self.backend._native
         st = ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
         P = self.backend._ptr
-        for b, (c, uz, cnt, ns) in enumerate(self.items):
-            key = (tuple(uz), ns)
-            plan = self.builders[key]._plan.handle
-            h = self.hist[key]
-            nat.call("emsim_gb300_bin_atoms_multi_slices", plan, P(c), int(c.shape[0]), P(cnt), P(h), st)
-            ws = self.ws[key]
-            nat.call("emsim_gb300_make_slices", plan, P(h), P(self.slices[b]), P(ws), ws.numel(), st)
+        nat.call("emsim_gb300_build_slices", self.builder._plan.handle, P(self.coords), self.n_atoms,
+                 P(self.counts), self.B, P(self.slices), P(self.ws), self.ws_bytes, st)
         W = WORKLOAD
         nat.call("emsim_gb300_multislice_image", self.wp._plan.handle, P(self.slices), self.ns,
                  self.ns * self.n * self.n, W["slice_thickness"], W["dose"], W["cs_mm"],

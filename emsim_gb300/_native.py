@@ -40,6 +40,11 @@ SIGNATURES = {
     "emsim_gb300_bin_atoms_multi_slices": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_vp, _c_vp]),
     "emsim_gb300_make_slices_workspace_size": (_c_size, [_c_vp]),
     "emsim_gb300_make_slices": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_build_slices_workspace_size": (_c_size, [_c_vp, _c_uint, _c_int]),
+    "emsim_gb300_build_slices": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_centralize": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "emsim_gb300_build_slices_z": (_c_int, [_c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_int,
+                                            _c_vp, _c_vp, _c_size, _c_vp]),
 }
 
 ERROR_NAMES = {1: "invalid argument", 2: "CUDA error", 3: "unsupported", 4: "wrong device"}

@@ -21,7 +21,8 @@ class AtomList:
 
     def __init__(self, elements: np.ndarray, coordinates: np.ndarray, label=""):
         self.elements = np.asarray(elements)
-        self.coordinates = np.asarray(coordinates).astype(float_type)
+        # float32 as the reference stores them; no copy when they already are
+        self.coordinates = np.asarray(coordinates).astype(float_type, copy=False)
         self.label = label
 
     @property

@@ -205,6 +205,81 @@ class MultiSlicesBuilder:
             self.unique_elements, self.n_slice, self.n1, self.n2, self.dz, self.d1, self.d2, False)[0]
         return _wrap(_make(plan, atom_histograms, self.n_slice, self.n1, self.n2))
 
+    @property
+    def atoms_path(self) -> bool:
+        """True when slices can be built straight from atoms (power-of-two sides 8..4096)."""
+        return all(n >= 8 and n <= 4096 and n & (n - 1) == 0 for n in (self.n1, self.n2))
+
+    def build_from_atoms(self, atom_coordinates_sorted_by_elems, unique_elements_count,
+                         symmetric_bandlimit: bool = True):
+        """make_multi_slices(bin_atoms_multi_slices(...)) without the dense histogram:
+        (n_slices, n1, n2) float32."""
+        return build_slices_batch(self, [(atom_coordinates_sorted_by_elems, unique_elements_count)],
+                                  symmetric_bandlimit)[0]
+
+
+def build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tensor, z: torch.Tensor,
+                                   offsets: torch.Tensor, shift: torch.Tensor, mol_index: Sequence[int], n_mol: int,
+                                   symmetric_bandlimit: bool = True) -> DeviceArray:
+    """Slices of molecules ``mol_index`` of a device-resident batch: ``xyz`` (n_atoms, 3)
+    float32, ``z`` (n_atoms) int32, ``offsets`` (n_mol + 1) uint32 atom offsets, ``shift``
+    (n_mol, 3) float32 per-molecule translation (centralisation).  Returns
+    (len(mol_index), n_slices, n1, n2) float32."""
+    plan = builder._plan if symmetric_bandlimit else slice_plan(
+        builder.unique_elements, builder.n_slice, builder.n1, builder.n2, builder.dz, builder.d1, builder.d2,
+        False)[0]
+    dev = _device()
+    slot = np.full(n_mol, -1, dtype=np.int32)
+    slot[list(mol_index)] = np.arange(len(mol_index), dtype=np.int32)
+    eoz = np.full(128, -1, dtype=np.int32)
+    for k, zz in enumerate(sorted(int(v) for v in builder.unique_elements)):
+        if 0 <= zz < 128:
+            eoz[zz] = k
+    meta = torch.from_numpy(np.concatenate([slot, eoz])).to(dev, non_blocking=True)
+    n_atoms = int(xyz.shape[0])
+    nb = len(mol_index)
+    out = torch.empty((nb, builder.n_slice, builder.n1, builder.n2), dtype=torch.float32, device=dev)
+    nbytes = int(_native.load().emsim_gb300_build_slices_workspace_size(plan.handle, n_atoms, nb))
+    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+    _native.call("emsim_gb300_build_slices_z", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets), n_mol,
+                 _ptr(shift), _ptr(meta), ctypes.c_void_p(meta.data_ptr() + 4 * n_mol), nb, _ptr(out), _ptr(ws),
+                 nbytes, _stream())
+    return _wrap(out)
+
+
+def build_slices_batch(builder: MultiSlicesBuilder, mols, symmetric_bandlimit: bool = True) -> DeviceArray:
+    """Slices of several molecules in one engine call.  ``mols``: sequence of
+    (coordinates sorted by element (N_b, 3), per-element counts in the builder's
+    element order).  Returns (B, n_slices, n1, n2) float32."""
+    if not builder.atoms_path:
+        return _wrap(torch.stack([builder.make_multi_slices(builder.bin_atoms_multi_slices(c, n), symmetric_bandlimit)
+                                  for c, n in mols]))
+    plan = builder._plan if symmetric_bandlimit else slice_plan(
+        builder.unique_elements, builder.n_slice, builder.n1, builder.n2, builder.dz, builder.d1, builder.d2,
+        False)[0]
+    dev = _device()
+    n_e = len(builder.unique_elements)
+    counts = np.zeros((len(mols), n_e), dtype=np.uint32)
+    parts = []
+    for i, (c, n) in enumerate(mols):
+        n = np.asarray(n).reshape(-1)
+        if n.shape[0] != n_e:
+            raise ValueError(f"unique_elements_count must have {n_e} entries, got {n.shape[0]}")
+        counts[i] = n
+        parts.append(np.asarray(c, dtype=np.float32).reshape(-1, 3) if not isinstance(c, torch.Tensor)
+                     else c.detach().to("cpu", torch.float32).numpy().reshape(-1, 3))
+    xyz = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros((0, 3), np.float32))
+    c_dev = as_device(xyz, torch.float32)
+    n_dev = as_device(counts.view(np.int32), torch.int32)
+    n_atoms = int(xyz.shape[0])
+    out = torch.empty((len(mols), builder.n_slice, builder.n1, builder.n2), dtype=torch.float32, device=dev)
+    lib = _native.load()
+    nbytes = int(lib.emsim_gb300_build_slices_workspace_size(plan.handle, n_atoms, len(mols)))
+    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+    _native.call("emsim_gb300_build_slices", plan.handle, _ptr(c_dev), n_atoms, _ptr(n_dev), len(mols), _ptr(out),
+                 _ptr(ws), nbytes, _stream())
+    return _wrap(out)
+
 
 # ---------------------------------------------------------------------------------
 # wave propagator

@@ -7,6 +7,8 @@
 #include <cmath>
 #include <vector>
 
+#include "atoms_sort.h"
+#include "binning.cuh"
 #include "slices.h"
 
 using namespace emsim_gb300;
@@ -20,6 +22,7 @@ struct emsim_gb300_slice_plan {
     float2* tw1 = nullptr;  // generic path twiddles exp(-2 pi i m / n)
     float2* tw2 = nullptr;
     float* filt = nullptr;  // (n_elems, n1, n2): F(k) * SF_e(k) / N
+    int2* wq = nullptr;     // fast path: W_n2^m = exp(-2 pi i m / n2) as 2^30-scaled fixed point
 };
 
 namespace {
@@ -79,36 +82,6 @@ int make_tw(int n, float2** out) {
 // ---------------------------------------------------------------------------------
 // binning (CUDA rule of SliceBuilder_kernel.cu:9-123)
 // ---------------------------------------------------------------------------------
-struct BinAxis {
-    float start, end, d;
-    int n;
-};
-
-// start = -d * floorf((float)(n + 1) / 2.0f); end = start + (float)n * d, which nvcc
-// contracts into one fused multiply-add (SliceBuilder_kernel.cu:30-34, 87-92).
-BinAxis make_axis(int n, double d) {
-    BinAxis a;
-    a.d = (float)d;
-    const float half = std::floor((float)(n + 1) / 2.0f);
-    a.start = -a.d * half;
-    a.end = std::fma((float)n, a.d, a.start);
-    a.n = n;
-    return a;
-}
-
-__device__ __forceinline__ bool bin_axis(float x, const BinAxis& ax, int& idx) {
-    if (!(ax.start <= x && x <= ax.end)) return false;
-    // LEFT_CLOSE: float difference compared against the double literal 1e-12
-    if ((double)__fsub_rn(ax.end, x) < 1e-12) {
-        idx = ax.n - 1;
-    } else {
-        int i = (int)floorf(__fdiv_rn(__fsub_rn(x, ax.start), ax.d));
-        // x a hair below end can round up to n; the reference then writes past the row
-        idx = i < ax.n ? i : ax.n - 1;
-    }
-    return true;
-}
-
 constexpr int MAX_ELEMS = 128;
 
 // One thread per atom.  Element of row r = number of cumulative counts <= r.  Counts
@@ -247,6 +220,40 @@ int generic_build(emsim_gb300_slice_plan* p, const SliceArgs& a, cudaStream_t st
     return EMSIM_GB300_OK;
 }
 
+// Workspace of build_slices for n_atoms atoms of n_img images, carved in this order
+// (each piece 256-byte aligned).
+struct AtomsWorkspace {
+    size_t group_start, group_tmp, bucket, item, count, off, cursor, bucket_tmp, items, work, total;
+    long long n_buckets;
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+AtomsWorkspace atoms_workspace(const emsim_gb300_slice_plan* p, unsigned n_atoms, int n_img) {
+    AtomsWorkspace w;
+    const long long n_groups = (long long)n_img * p->n_elems;
+    const long long pairs = (p->n_slices + 1) / 2;
+    w.n_buckets = n_groups * pairs * p->n1;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = align256(o + bytes);
+        return at;
+    };
+    w.group_start = take(sizeof(unsigned) * (n_groups + 1));
+    w.group_tmp = take(sizeof(unsigned) * scan_tmp_words(n_groups));
+    w.bucket = take(sizeof(unsigned) * (size_t)n_atoms);
+    w.item = take(sizeof(unsigned) * (size_t)n_atoms);
+    w.count = take(sizeof(unsigned) * (size_t)w.n_buckets);
+    w.off = take(sizeof(unsigned) * ((size_t)w.n_buckets + 1));
+    w.cursor = take(sizeof(unsigned) * (size_t)w.n_buckets);
+    w.bucket_tmp = take(sizeof(unsigned) * scan_tmp_words(w.n_buckets));
+    w.items = take(sizeof(unsigned) * (size_t)n_atoms);
+    w.work = take(sizeof(float2) * (size_t)n_img * pairs * p->n1 * p->n2);
+    w.total = o;
+    return w;
+}
+
 }  // namespace
 
 extern "C" {
@@ -273,6 +280,7 @@ int emsim_gb300_slice_plan_create(const float* sf_half, int n_elems, int n_slice
         cudaFree(p->tw1);
         cudaFree(p->tw2);
         cudaFree(p->filt);
+        cudaFree(p->wq);
         delete p;
         return code;
     };
@@ -306,6 +314,18 @@ int emsim_gb300_slice_plan_create(const float* sf_half, int n_elems, int n_slice
         set_error("slice plan: filter upload failed");
         return fail(EMSIM_GB300_ERR_CUDA);
     }
+    if (p->fast) {
+        std::vector<int2> wq(n2);
+        for (int m = 0; m < n2; ++m) {
+            const double ang = -2.0 * M_PI * (double)m / (double)n2;
+            wq[m] = make_int2((int)std::llrint(std::cos(ang) * 1073741824.0), (int)std::llrint(std::sin(ang) * 1073741824.0));
+        }
+        if (cudaMalloc((void**)&p->wq, sizeof(int2) * n2) != cudaSuccess ||
+            cudaMemcpy(p->wq, wq.data(), sizeof(int2) * n2, cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("slice plan: fixed-point twiddle upload failed");
+            return fail(EMSIM_GB300_ERR_CUDA);
+        }
+    }
     *plan = p;
     return EMSIM_GB300_OK;
 }
@@ -315,6 +335,7 @@ int emsim_gb300_slice_plan_destroy(emsim_gb300_slice_plan* p) {
     cudaFree(p->tw1);
     cudaFree(p->tw2);
     cudaFree(p->filt);
+    cudaFree(p->wq);
     delete p;
     return EMSIM_GB300_OK;
 }
@@ -333,6 +354,139 @@ size_t emsim_gb300_make_slices_workspace_size(const emsim_gb300_slice_plan* p) {
     if (!p) return 0;
     const size_t pairs = (size_t)(p->n_slices + 1) / 2;
     return sizeof(float2) * (size_t)p->n_elems * pairs * p->n1 * p->n2;
+}
+
+size_t emsim_gb300_build_slices_workspace_size(const emsim_gb300_slice_plan* p, unsigned n_atoms, int n_batch) {
+    if (!p || n_batch < 1) return 0;
+    return atoms_workspace(p, n_atoms, n_batch).total;
+}
+
+int emsim_gb300_build_slices(emsim_gb300_slice_plan* p, const float* coords, unsigned n_atoms,
+                             const uint32_t* elem_counts, int n_batch, float* out, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+    EMSIM_TRY(check_device(p));
+    EMSIM_REQUIRE(p->fast, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "build_slices: slice side is not a power of two in [8, 4096]; use bin_atoms + make_slices");
+    EMSIM_REQUIRE(n_batch >= 1 && out && elem_counts && workspace && (coords || n_atoms == 0),
+                  EMSIM_GB300_ERR_INVALID, "build_slices: bad arguments");
+    const AtomsWorkspace w = atoms_workspace(p, n_atoms, n_batch);
+    EMSIM_REQUIRE(workspace_bytes >= w.total, EMSIM_GB300_ERR_INVALID, "build_slices: workspace too small");
+    EMSIM_REQUIRE(((uintptr_t)workspace & 255) == 0, EMSIM_GB300_ERR_INVALID,
+                  "build_slices: workspace not 256-byte aligned");
+    EMSIM_REQUIRE(w.n_buckets < (long long)INVALID_BUCKET, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "build_slices: more than 2^32 - 1 (image, element, slice pair, row) buckets");
+    const long long pairs = (p->n_slices + 1) / 2;
+    EMSIM_REQUIRE((long long)n_batch * pairs <= 65535, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "build_slices: more than 65535 image x slice-pair planes per call");
+    cudaStream_t st = (cudaStream_t)stream;
+    char* base = (char*)workspace;
+    auto U = [&](size_t off) { return reinterpret_cast<unsigned*>(base + off); };
+    const int n_groups = n_batch * p->n_elems;
+    EMSIM_TRY(scan_u32(elem_counts, U(w.group_start), n_groups, U(w.group_tmp), st));
+    EMSIM_CHECK_CUDA(cudaMemsetAsync(U(w.count), 0, sizeof(unsigned) * (size_t)w.n_buckets, st));
+    AtomBucketArgs ba;
+    ba.coords = coords;
+    ba.n_atoms = n_atoms;
+    ba.group_start = U(w.group_start);
+    ba.n_groups = n_groups;
+    ba.n_pairs = (int)pairs;
+    ba.n1 = p->n1;
+    ba.ax0 = make_axis(p->n_slices, p->dz);
+    ba.ax1 = make_axis(p->n1, p->d1);
+    ba.ax2 = make_axis(p->n2, p->d2);
+    ba.bucket = U(w.bucket);
+    ba.item = U(w.item);
+    ba.bucket_count = U(w.count);
+    EMSIM_TRY(atoms_bucket(ba, st));
+    EMSIM_TRY(scan_u32(U(w.count), U(w.off), w.n_buckets, U(w.bucket_tmp), st));
+    EMSIM_CHECK_CUDA(cudaMemcpyAsync(U(w.cursor), U(w.off), sizeof(unsigned) * (size_t)w.n_buckets,
+                                     cudaMemcpyDeviceToDevice, st));
+    EMSIM_TRY(atoms_scatter(U(w.bucket), U(w.item), n_atoms, U(w.cursor), U(w.items), st));
+    SliceArgs a;
+    a.out = out;
+    a.work = reinterpret_cast<float2*>(base + w.work);
+    a.filt = p->filt;
+    a.tw = p->tw;
+    a.n_elems = p->n_elems;
+    a.n_slices = p->n_slices;
+    a.n_pairs = (int)pairs;
+    a.n1 = p->n1;
+    a.n2 = p->n2;
+    a.n_img = n_batch;
+    a.bucket_off = U(w.off);
+    a.items = U(w.items);
+    a.wq = p->wq;
+    return slice_atoms_build(a, st);
+}
+
+int emsim_gb300_centralize(const float* coords, const uint32_t* atom_offsets, int n_mol, float* shift_out,
+                           float* space_out, void* stream) {
+    EMSIM_REQUIRE(n_mol >= 0 && atom_offsets && shift_out && space_out && (coords || n_mol == 0),
+                  EMSIM_GB300_ERR_INVALID, "centralize: bad arguments");
+    return centralize(coords, atom_offsets, n_mol, shift_out, space_out, (cudaStream_t)stream);
+}
+
+int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* p, const float* coords, const int32_t* z, unsigned n_atoms,
+                               const uint32_t* atom_offsets, int n_mol, const float* shift, const int32_t* mol_slot,
+                               const int32_t* elem_of_z, int n_batch, float* out, void* workspace,
+                               size_t workspace_bytes, void* stream) {
+    EMSIM_TRY(check_device(p));
+    EMSIM_REQUIRE(p->fast, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "build_slices_z: slice side is not a power of two in [8, 4096]; use bin_atoms + make_slices");
+    EMSIM_REQUIRE(n_batch >= 1 && n_mol >= 1 && out && atom_offsets && shift && mol_slot && elem_of_z && workspace &&
+                      ((coords && z) || n_atoms == 0),
+                  EMSIM_GB300_ERR_INVALID, "build_slices_z: bad arguments");
+    const AtomsWorkspace w = atoms_workspace(p, n_atoms, n_batch);
+    EMSIM_REQUIRE(workspace_bytes >= w.total, EMSIM_GB300_ERR_INVALID, "build_slices_z: workspace too small");
+    EMSIM_REQUIRE(((uintptr_t)workspace & 255) == 0, EMSIM_GB300_ERR_INVALID,
+                  "build_slices_z: workspace not 256-byte aligned");
+    EMSIM_REQUIRE(w.n_buckets < (long long)INVALID_BUCKET, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "build_slices_z: more than 2^32 - 1 (image, element, slice pair, row) buckets");
+    const long long pairs = (p->n_slices + 1) / 2;
+    EMSIM_REQUIRE((long long)n_batch * pairs <= 65535, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "build_slices_z: more than 65535 image x slice-pair planes per call");
+    cudaStream_t st = (cudaStream_t)stream;
+    char* base = (char*)workspace;
+    auto U = [&](size_t off) { return reinterpret_cast<unsigned*>(base + off); };
+    EMSIM_CHECK_CUDA(cudaMemsetAsync(U(w.count), 0, sizeof(unsigned) * (size_t)w.n_buckets, st));
+    AtomBucketZArgs ba;
+    ba.coords = coords;
+    ba.z = z;
+    ba.n_atoms = n_atoms;
+    ba.atom_offsets = atom_offsets;
+    ba.n_mol = n_mol;
+    ba.shift = shift;
+    ba.mol_slot = mol_slot;
+    ba.elem_of_z = elem_of_z;
+    ba.n_elems = p->n_elems;
+    ba.n_pairs = (int)pairs;
+    ba.n1 = p->n1;
+    ba.ax0 = make_axis(p->n_slices, p->dz);
+    ba.ax1 = make_axis(p->n1, p->d1);
+    ba.ax2 = make_axis(p->n2, p->d2);
+    ba.bucket = U(w.bucket);
+    ba.item = U(w.item);
+    ba.bucket_count = U(w.count);
+    EMSIM_TRY(atoms_bucket_z(ba, st));
+    EMSIM_TRY(scan_u32(U(w.count), U(w.off), w.n_buckets, U(w.bucket_tmp), st));
+    EMSIM_CHECK_CUDA(cudaMemcpyAsync(U(w.cursor), U(w.off), sizeof(unsigned) * (size_t)w.n_buckets,
+                                     cudaMemcpyDeviceToDevice, st));
+    EMSIM_TRY(atoms_scatter(U(w.bucket), U(w.item), n_atoms, U(w.cursor), U(w.items), st));
+    SliceArgs a;
+    a.out = out;
+    a.work = reinterpret_cast<float2*>(base + w.work);
+    a.filt = p->filt;
+    a.tw = p->tw;
+    a.n_elems = p->n_elems;
+    a.n_slices = p->n_slices;
+    a.n_pairs = (int)pairs;
+    a.n1 = p->n1;
+    a.n2 = p->n2;
+    a.n_img = n_batch;
+    a.bucket_off = U(w.off);
+    a.items = U(w.items);
+    a.wq = p->wq;
+    return slice_atoms_build(a, st);
 }
 
 int emsim_gb300_make_slices(emsim_gb300_slice_plan* p, const float* hist, float* out, void* workspace,

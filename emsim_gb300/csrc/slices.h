@@ -12,8 +12,16 @@ struct SliceArgs {
     const float* filt = nullptr;  // (n_elems, n1, n2) real: band-limit * SF_e / N
     const float2* tw = nullptr;   // FFT twiddle table of the device
     int n_elems = 0, n_slices = 0, n_pairs = 0, n1 = 0, n2 = 0;
+    int n_img = 1;  // slice stacks in the call (work / out hold n_img stacks back to back)
+    // bucketed atoms (build from atoms)
+    const unsigned* bucket_off = nullptr;  // (n_img * n_elems * n_pairs * n1 + 1) start offsets into items
+    const unsigned* items = nullptr;       // (slice parity << 31) | column, grouped by bucket
+    const int2* wq = nullptr;              // W_n2^m, m < n2, as 2^30-scaled fixed point
 };
 
+// dense histogram -> slices (three passes)
 int slice_fast_build(const SliceArgs& a, cudaStream_t st);
+// bucketed atoms -> slices (column pass from atoms + inverse row pass)
+int slice_atoms_build(const SliceArgs& a, cudaStream_t st);
 
 }  // namespace emsim_gb300

@@ -1,146 +1,7 @@
-// Projected-potential slices on the power-of-two fast path.
-//
-// The reference (SliceBuilder.cu:108-133 + slice_builder_cuda.py:88-99) runs an R2C per
-// (element, slice), a broadcast multiply by the scattering factors, a multi-pass element
-// reduction, a C2R, then a second R2C/C2R pair for the band-limit and a clip.  All of
-// that is linear and the filters are real and symmetric, so here
-//   V_s + i V_{s+1} = IFFT2( sum_e T_e(k) * FFT2(h_{e,s} + i h_{e,s+1}) )
-// with T_e = F(k) * SF_e(k) / N (F = band-limit, symmetrised exactly as the C2R of the
-// reference sees it).  Two slices share each complex transform and the element sum,
-// multiply and band-limit happen in registers between the forward and inverse column
-// FFTs.  Three passes over HBM:
-//   A  rows   : hist pair (2 x float) -> forward row FFT -> Z[e, pair]       (complex)
-//   B  columns: for each e: fwd col FFT of Z[e, pair], accumulate T_e * Zhat;
-//               inverse col FFT -> W[pair] (written over Z[0, pair])
-//   C  rows   : W[pair] -> inverse row FFT -> clip(re) -> V[2p], clip(im) -> V[2p+1]
-#include "slices.h"
-#include "wave_passes.cuh"
+// Size dispatch of the projected-potential slice passes (kernels in slice_passes.cuh).
+#include "slice_passes.cuh"
 
 namespace emsim_gb300 {
-
-template <int N>
-__global__ void __launch_bounds__(512) slice_rows_fwd_kernel(SliceArgs a) {
-    constexpr int T = N / 8;
-    constexpr bool WARP_ONLY = (T <= 32);
-    extern __shared__ float2 sm[];
-    const int b = threadIdx.x / T;
-    const int t = threadIdx.x - b * T;
-    const int B = blockDim.x / T;
-    const int row = blockIdx.x * B + b;
-    const int img = blockIdx.y;  // e * n_pairs + pair
-    const int e = img / a.n_pairs;
-    const int pair = img - e * a.n_pairs;
-    const long long npix = (long long)a.n1 * N;
-    const int s0 = 2 * pair, s1 = 2 * pair + 1;
-    const float* h0 = a.hist + ((long long)e * a.n_slices + s0) * npix + (long long)row * N;
-    const float* h1 = s1 < a.n_slices ? a.hist + ((long long)e * a.n_slices + s1) * npix + (long long)row * N : nullptr;
-    float2 v[8];
-#pragma unroll
-    for (int m = 0; m < 8; ++m) v[m] = make_float2(__ldg(h0 + t + m * T), h1 ? __ldg(h1 + t + m * T) : 0.f);
-    fft::fft_regs<N, false, WARP_ONLY>(v, sm, b, t, RowAddr<N>{}, a.tw);
-    float2* dst = a.work + (long long)img * npix + (long long)row * N;
-#pragma unroll
-    for (int m = 0; m < 8; ++m) dst[t + m * T] = v[m];
-}
-
-template <int N>
-__global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS) slice_cols_kernel(SliceArgs a) {
-    constexpr int T = N / 8;
-    extern __shared__ float2 sm[];
-    const int B = blockDim.x / T;
-    const int b = threadIdx.x & (B - 1);
-    const int t = threadIdx.x / B;
-    const int col = blockIdx.x * B + b;
-    const int pair = blockIdx.y;
-    const long long npix = (long long)N * a.n2;
-    const long long ld = a.n2;
-    ColAddrRt addr{B};
-    float2 acc[8];
-#pragma unroll
-    for (int m = 0; m < 8; ++m) acc[m] = make_float2(0.f, 0.f);
-    for (int e = 0; e < a.n_elems; ++e) {
-        const float2* src = a.work + ((long long)e * a.n_pairs + pair) * npix + col;
-        float2 v[8];
-#pragma unroll
-        for (int m = 0; m < 8; ++m) v[m] = src[(long long)(t + m * T) * ld];
-        fft::fft_regs<N, false, false>(v, sm, b, t, addr, a.tw);
-        const float* te = a.filt + (long long)e * npix + col;
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            const float w = __ldg(te + (long long)(t + m * T) * ld);
-            acc[m].x = fmaf(w, v[m].x, acc[m].x);
-            acc[m].y = fmaf(w, v[m].y, acc[m].y);
-        }
-    }
-    fft::fft_regs<N, true, false>(acc, sm, b, t, addr, a.tw);
-    float2* dst = a.work + (long long)pair * npix + col;  // element 0's slot of this pair
-#pragma unroll
-    for (int m = 0; m < 8; ++m) dst[(long long)(t + m * T) * ld] = acc[m];
-}
-
-__device__ __forceinline__ float clip_low(float v) { return v < 1e-13f ? 1e-13f : v; }
-
-template <int N>
-__global__ void __launch_bounds__(512) slice_rows_inv_kernel(SliceArgs a) {
-    constexpr int T = N / 8;
-    constexpr bool WARP_ONLY = (T <= 32);
-    extern __shared__ float2 sm[];
-    const int b = threadIdx.x / T;
-    const int t = threadIdx.x - b * T;
-    const int B = blockDim.x / T;
-    const int row = blockIdx.x * B + b;
-    const int pair = blockIdx.y;
-    const long long npix = (long long)a.n1 * N;
-    const float2* src = a.work + (long long)pair * npix + (long long)row * N;
-    float2 v[8];
-#pragma unroll
-    for (int m = 0; m < 8; ++m) v[m] = src[t + m * T];
-    fft::fft_regs<N, true, WARP_ONLY>(v, sm, b, t, RowAddr<N>{}, a.tw);
-    const int s0 = 2 * pair, s1 = 2 * pair + 1;
-    float* o0 = a.out + (long long)s0 * npix + (long long)row * N;
-#pragma unroll
-    for (int m = 0; m < 8; ++m) o0[t + m * T] = clip_low(v[m].x);
-    if (s1 < a.n_slices) {
-        float* o1 = a.out + (long long)s1 * npix + (long long)row * N;
-#pragma unroll
-        for (int m = 0; m < 8; ++m) o1[t + m * T] = clip_low(v[m].y);
-    }
-}
-
-template <int N>
-static int rows_launch(void (*k)(SliceArgs), const SliceArgs& a, int n_rows, int n_img, cudaStream_t st) {
-    constexpr int T = N / 8;
-    int threads = row_threads(N);
-    int B = threads / T;
-    if (B > n_rows) B = n_rows;
-    threads = B * T;
-    const size_t smem = (size_t)fft::RowLayout<N>::words(B) * sizeof(float2);
-    EMSIM_TRY(ensure_smem_attr((const void*)k, smem));
-    k<<<dim3(n_rows / B, n_img), threads, smem, st>>>(a);
-    EMSIM_CHECK_LAUNCH();
-    return EMSIM_GB300_OK;
-}
-
-// Pass A on rows of length n2 (= N here)
-template <int N>
-int slice_rows_fwd_n(const SliceArgs& a, cudaStream_t st) {
-    return rows_launch<N>(slice_rows_fwd_kernel<N>, a, a.n1, a.n_elems * a.n_pairs, st);
-}
-template <int N>
-int slice_rows_inv_n(const SliceArgs& a, cudaStream_t st) {
-    return rows_launch<N>(slice_rows_inv_kernel<N>, a, a.n1, a.n_pairs, st);
-}
-// Pass B on columns of length n1 (= N here)
-template <int N>
-int slice_cols_n(const SliceArgs& a, cudaStream_t st) {
-    constexpr int T = N / 8;
-    const int B = col_B_for(N, a.n2);
-    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2);
-    EMSIM_TRY(ensure_smem_attr((const void*)slice_cols_kernel<N>, smem));
-    slice_cols_kernel<N><<<dim3(a.n2 / B, a.n_pairs), B * T, smem, st>>>(a);
-    EMSIM_CHECK_LAUNCH();
-    return EMSIM_GB300_OK;
-}
 
 #define EMSIM_SLICE_SIZES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 
@@ -165,6 +26,24 @@ int slice_fast_build(const SliceArgs& a, cudaStream_t st) {
         EMSIM_SLICE_SIZES(EMSIM_CASE)
 #undef EMSIM_CASE
     }
+    return EMSIM_GB300_ERR_UNSUPPORTED;
+}
+
+int slice_atoms_build(const SliceArgs& a, cudaStream_t st) {
+    switch (a.n1) {
+#define EMSIM_CASE(N) \
+    case N: EMSIM_TRY(slice_cols_atoms_n<N>(a, st)); break;
+        EMSIM_SLICE_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
+        default: set_error("slice build: column length not on the fast path"); return EMSIM_GB300_ERR_UNSUPPORTED;
+    }
+    switch (a.n2) {
+#define EMSIM_CASE(N) \
+    case N: return slice_rows_inv_n<N>(a, st);
+        EMSIM_SLICE_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
+    }
+    set_error("slice build: row length not on the fast path");
     return EMSIM_GB300_ERR_UNSUPPORTED;
 }
 

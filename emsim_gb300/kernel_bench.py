@@ -10,7 +10,8 @@ ncu captures of single kernels.
 
 cases: step (multislice_propagate), space (space_propagate), lens (lens_propagate),
 image (multislice_image: plane wave -> slices -> lens -> |psi|^2), slices
-(make_multi_slices), bin (bin_atoms_multi_slices).
+(make_multi_slices), atoms (build_slices: slices straight from atoms, --atoms per image),
+bin (bin_atoms_multi_slices).
 """
 from __future__ import annotations
 
@@ -39,7 +40,7 @@ def _time(fn, reps: int, flush: torch.Tensor) -> float:
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="step", choices=["step", "space", "lens", "image", "slices", "bin"])
+    ap.add_argument("--case", default="step", choices=["step", "space", "lens", "image", "slices", "atoms", "bin"])
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--slices", type=int, default=4)
@@ -101,6 +102,25 @@ def main(argv=None):
         t = _time(fn, args.reps, flush)
         out.update(elements=E, slices=S, seconds=t, slices_per_s=S / t,
                    algo_gbs=(4.0 * E + 4.0) * S * n * n / t / 1e9)
+    elif args.case == "atoms":
+        zs = [6, 7, 8, 16]
+        b = backend.MultiSlicesBuilder(zs, S, n, n, 2.0, 1.0, 1.0)
+        rng = np.random.default_rng(0)
+        N = args.atoms * B
+        xyz = ((rng.random((N, 3)) * 2 - 1) * np.array([S, n / 2, n / 2]) * 0.9).astype(np.float32)
+        per = np.array([args.atoms // 4] * 3 + [args.atoms - 3 * (args.atoms // 4)], dtype=np.uint32)
+        counts = np.tile(per, (B, 1))
+        c = torch.from_numpy(xyz).to(dev)
+        cn = torch.from_numpy(counts.view(np.int32)).to(dev)
+        o = torch.empty((B, S, n, n), dtype=torch.float32, device=dev)
+        nbytes = int(_native.load().emsim_gb300_build_slices_workspace_size(b._plan.handle, N, B))
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        fn = lambda: _native.call("emsim_gb300_build_slices", b._plan.handle, P(c), N, P(cn), B, P(o), P(ws),  # noqa
+                                  nbytes, st())
+        for _ in range(args.warmup):
+            fn()
+        t = _time(fn, args.reps, flush)
+        out.update(batch=B, atoms=N, slices=S, seconds=t, images_per_s=B / t, slices_per_s=B * S / t)
     else:
         zs = [6, 7, 8, 16]
         b = backend.MultiSlicesBuilder(zs, S, n, n, 2.0, 1.0, 1.0)

@@ -75,19 +75,97 @@ class Pipe:
 
     def run(self, mol):
         """Image of one molecule, (n1, n2) float32 on the device."""
+        if not self.add_water:
+            return self.run_batch([mol])[0]
         slices = self.build_slices(mol)
         m = self.microscope
         wp = self._propagator(slices.shape[-2:])
         return wp.image(slices, self.slice_thickness, m.electron_dose, m.cs_mm, m.defocus, m.aperture)
 
+    def _geometry(self, mol: atm.AtomList):
+        """Centralize, group by element and size the slice stack (pot.py:29-48)."""
+        mol = atm.centralize(mol)
+        must = [1, 8] if self.add_water else []
+        mol, uz, cnt = atm.sort_elements_and_count(mol, must)
+        ns, n1, n2 = pot.finalize_slice_size(tuple(mol.space), (self._pixel_size, self._pixel_size),
+                                             self.slice_thickness, self.roi, None)
+        return mol, uz, cnt, (ns, n1, n2)
+
+    def _stage(self, n_atoms: int):
+        """Pinned host staging buffers (grown on demand) for coordinates and Z."""
+        if getattr(self, "_pin_xyz", None) is None or self._pin_xyz.shape[0] < n_atoms:
+            cap = max(n_atoms, 1024)
+            self._pin_xyz = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True)
+            self._pin_z = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+        return self._pin_xyz[:n_atoms], self._pin_z[:n_atoms]
+
     def run_batch(self, mols: Sequence[atm.AtomList], defocus: Optional[Sequence[float]] = None) -> List:
-        """Images of many molecules (optionally one defocus each), in input order."""
+        """Images of many molecules (optionally one defocus each), in input order.
+
+        The molecules travel to the device once; centralisation, grouping by element,
+        binning and slice building run there (emsim_gb300_centralize, build_slices_z).
+        Only the per-molecule extents come back to size the slice stacks.  Molecules with
+        the same stack shape share one slice-build call and one image-formation call;
+        each group uses the union of its molecules' elements (an absent element adds
+        exactly zero to a slice)."""
+        if self.add_water:
+            return self._run_batch_host(mols, defocus)
         m = self.microscope
-        built = [self.build_slices(mol) for mol in mols]
+        dev = backend._device()
+        sizes = [len(mol.elements) for mol in mols]
+        if any(s == 0 for s in sizes):
+            raise ValueError("zero-size array to reduction operation minimum which has no identity")
+        offsets = np.zeros(len(mols) + 1, dtype=np.int64)
+        offsets[1:] = np.cumsum(sizes)
+        n_atoms = int(offsets[-1])
+        hx, hz = self._stage(n_atoms)
+        nx, nz = hx.numpy(), hz.numpy()
+        present = np.zeros((len(mols), 128), dtype=bool)
+        for i, mol in enumerate(mols):
+            nx[offsets[i]:offsets[i + 1]] = mol.coordinates
+            z = np.asarray(mol.elements)
+            nz[offsets[i]:offsets[i + 1]] = z
+            zk = z[(z >= 0) & (z < 128)]
+            present[i] = np.bincount(zk, minlength=128)[:128] > 0
+        xyz = hx.to(dev, non_blocking=True)
+        zz = hz.to(dev, non_blocking=True)
+        off = torch.from_numpy(offsets.astype(np.uint32).view(np.int32)).to(dev)
+        shift = torch.empty((len(mols), 3), dtype=torch.float32, device=dev)
+        space = torch.empty((len(mols), 3), dtype=torch.float32, device=dev)
+        st = backend._stream()
+        backend._native.call("emsim_gb300_centralize", backend._ptr(xyz), backend._ptr(off), len(mols),
+                             backend._ptr(shift), backend._ptr(space), st)
+        space_h = space.cpu().numpy()
         groups = defaultdict(list)
-        for i, s in enumerate(built):
-            groups[tuple(s.shape)].append(i)
+        for i in range(len(mols)):
+            shape = pot.finalize_slice_size(tuple(space_h[i]), (self._pixel_size, self._pixel_size),
+                                            self.slice_thickness, self.roi, None)
+            groups[shape].append(i)
         out: List = [None] * len(mols)
+        for (ns, n1, n2), idx in groups.items():
+            uz = [int(z) for z in np.nonzero(present[idx].any(axis=0))[0]]
+            b = backend.MultiSlicesBuilder(uz, ns, n1, n2, self.slice_thickness, self._pixel_size, self._pixel_size)
+            if b.atoms_path:
+                stack = backend.build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, len(mols))
+            else:
+                stack = torch.stack([self.build_slices(mols[i]) for i in idx])
+            dfs = [m.defocus if defocus is None else defocus[i] for i in idx]
+            wp = self._propagator((n1, n2))
+            imgs = wp.image(stack, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture)
+            for j, i in enumerate(idx):
+                out[i] = imgs[j]
+        return out
+
+    def _run_batch_host(self, mols, defocus=None) -> List:
+        """run_batch with the front-end on the host (voxel water needs the histograms)."""
+        m = self.microscope
+        out: List = [None] * len(mols)
+        groups = defaultdict(list)
+        built = {}
+        for i, mol in enumerate(mols):
+            s = self.build_slices(mol)
+            built[i] = s
+            groups[tuple(s.shape)].append(i)
         for shape, idx in groups.items():
             stack = torch.stack([built[i] for i in idx])
             dfs = [m.defocus if defocus is None else defocus[i] for i in idx]

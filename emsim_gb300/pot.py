@@ -46,6 +46,9 @@ def build_multi_slices(mol: atm.AtomList, dz: float, pixel_size: Union[float, Tu
     mol, uz, cnt = atm.sort_elements_and_count(mol, must)
     ns, n1, n2 = finalize_slice_size(tuple(mol.space), pixel_size, dz, lateral_size, n_slices)
     b = backend.MultiSlicesBuilder(list(uz), ns, n1, n2, dz, pixel_size[0], pixel_size[1])
+    if not add_water and b.atoms_path:
+        # same bins and slices without the dense histogram
+        return b.build_from_atoms(mol.coordinates, cnt)
     h = b.bin_atoms_multi_slices(mol.coordinates, cnt)
     if add_water:
         h = b.add_water(h)

@@ -145,6 +145,44 @@ size_t emsim_gb300_make_slices_workspace_size(const emsim_gb300_slice_plan* plan
 int emsim_gb300_make_slices(emsim_gb300_slice_plan* plan, const float* hist, float* out, void* workspace,
                             size_t workspace_bytes, void* stream);
 
+/* Bytes of device workspace emsim_gb300_build_slices needs for n_atoms atoms of
+ * n_batch molecules. */
+size_t emsim_gb300_build_slices_workspace_size(const emsim_gb300_slice_plan* plan, unsigned n_atoms, int n_batch);
+
+/* Slices of n_batch molecules straight from their atoms: the composition
+ * make_slices(bin_atoms_multi_slices(...)) of pot.build_multi_slices (pot.py:29-48,
+ * slice_builder_cuda.py:63-70) without materialising the (n_elems, n_slices, n1, n2)
+ * histogram.  Atoms are binned with the same rule, counting-sorted into
+ * (molecule, element, slice pair, row) buckets, and the row transforms of the binned
+ * atoms are summed exactly in 64-bit fixed point, so the result is deterministic.
+ * coords: (n_atoms, 3) float32 device, molecules back to back, each grouped by element;
+ * elem_counts: (n_batch, n_elems) uint32 device; out: (n_batch, n_slices, n1, n2) float32.
+ * Needs n1, n2 powers of two in [8, 4096] (else EMSIM_GB300_ERR_UNSUPPORTED). */
+int emsim_gb300_build_slices(emsim_gb300_slice_plan* plan, const float* coords, unsigned n_atoms,
+                             const uint32_t* elem_counts, int n_batch, float* out, void* workspace,
+                             size_t workspace_bytes, void* stream);
+
+/* Centralisation of n_mol molecules on the device (atoms.centralize, emsim/atoms.py:142-159,
+ * and AtomList.space, atoms.py:37-47): for each molecule, shift = -r_min - (r_max - r_min)/2
+ * and the extent of the shifted coordinates, in float32 exactly as numpy evaluates them.
+ * coords: (n_atoms, 3) float32 device; atom_offsets: (n_mol + 1) uint32 device, molecule m
+ * owning atoms [off[m], off[m + 1]) (every molecule non-empty); shift_out, space_out:
+ * (n_mol, 3) float32 device. */
+int emsim_gb300_centralize(const float* coords, const uint32_t* atom_offsets, int n_mol, float* shift_out,
+                           float* space_out, void* stream);
+
+/* emsim_gb300_build_slices for molecules given as they come (pot.build_multi_slices after
+ * atoms.centralize, pipe.py:46-52): atoms in any order with their atomic numbers z
+ * (n_atoms) int32; molecule m's coordinates are shifted by shift[m] (float32 add, e.g. the
+ * output of emsim_gb300_centralize) before binning and go to output image mol_slot[m]
+ * (-1: skip); elem_of_z: (128) int32 device table, element index of each Z in the plan's
+ * element order or -1 (atoms of absent elements are dropped).  Workspace as for
+ * emsim_gb300_build_slices_workspace_size(plan, n_atoms, n_batch). */
+int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* plan, const float* coords, const int32_t* z, unsigned n_atoms,
+                               const uint32_t* atom_offsets, int n_mol, const float* shift, const int32_t* mol_slot,
+                               const int32_t* elem_of_z, int n_batch, float* out, void* workspace,
+                               size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
