@@ -162,6 +162,23 @@ int emsim_gb300_build_slices(emsim_gb300_slice_plan* plan, const float* coords, 
                              const uint32_t* elem_counts, int n_batch, float* out, void* workspace,
                              size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------------
+ * Slices without a workspace.  No counterpart in the reference.
+ * For callers that cannot allocate device memory when they need slices - a plugin inside
+ * a host program that owns all device memory through its own pool, or a loop that must
+ * not allocate after start-up (cudaMalloc/cudaFree can synchronise the device).  Same
+ * result as emsim_gb300_make_slices, with the intermediate kept in one static device
+ * buffer of EMSIM_GB300_NOALLOC_SCRATCH_BYTES instead of a workspace; no cudaMalloc,
+ * cudaFree or allocating library call.  A plan needing more scratch
+ * (emsim_gb300_make_slices_workspace_size) is rejected with EMSIM_GB300_ERR_UNSUPPORTED.
+ * Every GPU that loads this part of the library may hold the buffer until the process
+ * exits.  All calls on a device share it and it keeps the last call's contents (nothing
+ * in it needs to start at zero); calls that overlap on the GPU race on it.  The first
+ * call on a device looks up the buffer's address; make it before any stream capture.
+ * ------------------------------------------------------------------------------- */
+#define EMSIM_GB300_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int emsim_gb300_make_slices_noalloc(emsim_gb300_slice_plan* plan, const float* hist, float* out, void* stream);
+
 /* Centralisation of n_mol molecules on the device (atoms.centralize, emsim/atoms.py:142-159,
  * and AtomList.space, atoms.py:37-47): for each molecule, shift = -r_min - (r_max - r_min)/2
  * and the extent of the shifted coordinates, in float32 exactly as numpy evaluates them.
