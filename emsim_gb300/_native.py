@@ -43,7 +43,7 @@ SIGNATURES = {
     "emsim_gb300_build_slices_workspace_size": (_c_size, [_c_vp, _c_uint, _c_int]),
     "emsim_gb300_build_slices": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
     "emsim_gb300_make_slices_noalloc": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
-    "emsim_gb300_centralize": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "emsim_gb300_centralize": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "emsim_gb300_build_slices_z": (_c_int, [_c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_int,
                                             _c_vp, _c_vp, _c_size, _c_vp]),
 }

@@ -184,11 +184,24 @@ int atoms_bucket_z(const AtomBucketZArgs& a, cudaStream_t st) {
     return EMSIM_GB300_OK;
 }
 
-// one block per molecule; min/max are exact, so the result does not depend on order
-__global__ void centralize_kernel(const float* coords, const unsigned* off, float* shift, float* space) {
+// one block per molecule; min/max are exact, so the result does not depend on order.
+// With z != nullptr also a 128-bit mask of the atomic numbers present (Z < 128).
+__global__ void centralize_kernel(const float* coords, const int* z, const unsigned* off, float* shift, float* space,
+                                  unsigned* present) {
     __shared__ float red[6][32];
+    __shared__ unsigned mask[4];
     const int m = blockIdx.x;
     const unsigned a0 = off[m], a1 = off[m + 1];
+    if (z) {
+        if (threadIdx.x < 4) mask[threadIdx.x] = 0u;
+        __syncthreads();
+        for (unsigned r = a0 + threadIdx.x; r < a1; r += blockDim.x) {
+            const int zz = z[r];
+            if (zz >= 0 && zz < 128) atomicOr(&mask[zz >> 5], 1u << (zz & 31));
+        }
+        __syncthreads();
+        if (threadIdx.x < 4) present[4 * m + threadIdx.x] = mask[threadIdx.x];
+    }
     float sh[3];
     for (int pass = 0; pass < 2; ++pass) {
         float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -238,10 +251,10 @@ __global__ void centralize_kernel(const float* coords, const unsigned* off, floa
     }
 }
 
-int centralize(const float* coords, const unsigned* atom_offsets, int n_mol, float* shift, float* space,
-               cudaStream_t st) {
+int centralize(const float* coords, const int* z, const unsigned* atom_offsets, int n_mol, float* shift, float* space,
+               unsigned* present, cudaStream_t st) {
     if (n_mol <= 0) return EMSIM_GB300_OK;
-    centralize_kernel<<<n_mol, 256, 0, st>>>(coords, atom_offsets, shift, space);
+    centralize_kernel<<<n_mol, 256, 0, st>>>(coords, present ? z : nullptr, atom_offsets, shift, space, present);
     EMSIM_CHECK_LAUNCH();
     return EMSIM_GB300_OK;
 }

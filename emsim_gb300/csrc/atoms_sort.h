@@ -41,9 +41,10 @@ struct AtomBucketZArgs {
 int atoms_bucket_z(const AtomBucketZArgs& a, cudaStream_t st);
 
 // per molecule: shift = -r_min - (r_max - r_min) / 2 and the extent of the shifted
-// coordinates, both float32 as emsim/atoms.py:37-47, 142-159 evaluate them
-int centralize(const float* coords, const unsigned* atom_offsets, int n_mol, float* shift, float* space,
-               cudaStream_t st);
+// coordinates, both float32 as emsim/atoms.py:37-47, 142-159 evaluate them; with
+// present != nullptr also the 128-bit mask (4 words) of atomic numbers z present
+int centralize(const float* coords, const int* z, const unsigned* atom_offsets, int n_mol, float* shift, float* space,
+               unsigned* present, cudaStream_t st);
 
 // exclusive scan of n unsigned values into out[0..n]; out[n] = total; tmp holds
 // scan_tmp_words(n) words

@@ -419,11 +419,12 @@ int emsim_gb300_build_slices(emsim_gb300_slice_plan* p, const float* coords, uns
     return slice_atoms_build(a, st);
 }
 
-int emsim_gb300_centralize(const float* coords, const uint32_t* atom_offsets, int n_mol, float* shift_out,
-                           float* space_out, void* stream) {
-    EMSIM_REQUIRE(n_mol >= 0 && atom_offsets && shift_out && space_out && (coords || n_mol == 0),
+int emsim_gb300_centralize(const float* coords, const int32_t* z, const uint32_t* atom_offsets, int n_mol,
+                           float* shift_out, float* space_out, uint32_t* present_out, void* stream) {
+    EMSIM_REQUIRE(n_mol >= 0 && atom_offsets && shift_out && space_out && (coords || n_mol == 0) &&
+                      (present_out == nullptr || z != nullptr),
                   EMSIM_GB300_ERR_INVALID, "centralize: bad arguments");
-    return centralize(coords, atom_offsets, n_mol, shift_out, space_out, (cudaStream_t)stream);
+    return centralize(coords, z, atom_offsets, n_mol, shift_out, space_out, present_out, (cudaStream_t)stream);
 }
 
 int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* p, const float* coords, const int32_t* z, unsigned n_atoms,

@@ -76,7 +76,7 @@ class Pipe:
     def run(self, mol):
         """Image of one molecule, (n1, n2) float32 on the device."""
         if not self.add_water:
-            return self.run_batch([mol])[0]
+            return backend._wrap(self.run_batch([mol])[0])
         slices = self.build_slices(mol)
         m = self.microscope
         wp = self._propagator(slices.shape[-2:])
@@ -99,59 +99,64 @@ class Pipe:
             self._pin_z = torch.empty(cap, dtype=torch.int32, pin_memory=True)
         return self._pin_xyz[:n_atoms], self._pin_z[:n_atoms]
 
-    def run_batch(self, mols: Sequence[atm.AtomList], defocus: Optional[Sequence[float]] = None) -> List:
+    def run_batch(self, mols: Sequence[atm.AtomList], defocus: Optional[Sequence[float]] = None,
+                  to_host: bool = False) -> List:
         """Images of many molecules (optionally one defocus each), in input order.
 
-        The molecules travel to the device once; centralisation, grouping by element,
-        binning and slice building run there (emsim_gb300_centralize, build_slices_z).
-        Only the per-molecule extents come back to size the slice stacks.  Molecules with
-        the same stack shape share one slice-build call and one image-formation call;
-        each group uses the union of its molecules' elements (an absent element adds
-        exactly zero to a slice)."""
+        The molecules travel to the device once; centralisation, element sets, binning
+        and slice building run there (emsim_gb300_centralize, build_slices_z).  Only the
+        per-molecule extents and element masks come back to size the slice stacks.
+        Molecules with the same stack shape share one slice-build call and one
+        image-formation call; each group uses the union of its molecules' elements (an
+        absent element adds exactly zero to a slice).  ``to_host``: return numpy images,
+        copied with one transfer per group."""
         if self.add_water:
-            return self._run_batch_host(mols, defocus)
+            imgs = self._run_batch_host(mols, defocus)
+            return [im.get() for im in imgs] if to_host else imgs
         m = self.microscope
         dev = backend._device()
         sizes = [len(mol.elements) for mol in mols]
         if any(s == 0 for s in sizes):
             raise ValueError("zero-size array to reduction operation minimum which has no identity")
-        offsets = np.zeros(len(mols) + 1, dtype=np.int64)
+        nm = len(mols)
+        offsets = np.zeros(nm + 1, dtype=np.int64)
         offsets[1:] = np.cumsum(sizes)
         n_atoms = int(offsets[-1])
         hx, hz = self._stage(n_atoms)
         nx, nz = hx.numpy(), hz.numpy()
-        present = np.zeros((len(mols), 128), dtype=bool)
         for i, mol in enumerate(mols):
             nx[offsets[i]:offsets[i + 1]] = mol.coordinates
-            z = np.asarray(mol.elements)
-            nz[offsets[i]:offsets[i + 1]] = z
-            zk = z[(z >= 0) & (z < 128)]
-            present[i] = np.bincount(zk, minlength=128)[:128] > 0
+            nz[offsets[i]:offsets[i + 1]] = mol.elements
         xyz = hx.to(dev, non_blocking=True)
         zz = hz.to(dev, non_blocking=True)
         off = torch.from_numpy(offsets.astype(np.uint32).view(np.int32)).to(dev)
-        shift = torch.empty((len(mols), 3), dtype=torch.float32, device=dev)
-        space = torch.empty((len(mols), 3), dtype=torch.float32, device=dev)
-        st = backend._stream()
-        backend._native.call("emsim_gb300_centralize", backend._ptr(xyz), backend._ptr(off), len(mols),
-                             backend._ptr(shift), backend._ptr(space), st)
+        shift = torch.empty((nm, 3), dtype=torch.float32, device=dev)
+        space = torch.empty((nm, 3), dtype=torch.float32, device=dev)
+        present = torch.empty((nm, 4), dtype=torch.int32, device=dev)
+        P = backend._ptr
+        backend._native.call("emsim_gb300_centralize", P(xyz), P(zz), P(off), nm, P(shift), P(space), P(present),
+                             backend._stream())
         space_h = space.cpu().numpy()
+        mask_h = present.cpu().numpy().view(np.uint32)
         groups = defaultdict(list)
-        for i in range(len(mols)):
+        for i in range(nm):
             shape = pot.finalize_slice_size(tuple(space_h[i]), (self._pixel_size, self._pixel_size),
                                             self.slice_thickness, self.roi, None)
             groups[shape].append(i)
-        out: List = [None] * len(mols)
+        out: List = [None] * nm
         for (ns, n1, n2), idx in groups.items():
-            uz = [int(z) for z in np.nonzero(present[idx].any(axis=0))[0]]
+            union = np.bitwise_or.reduce(mask_h[idx], axis=0)
+            uz = [32 * w + b for w in range(4) for b in range(32) if (int(union[w]) >> b) & 1]
             b = backend.MultiSlicesBuilder(uz, ns, n1, n2, self.slice_thickness, self._pixel_size, self._pixel_size)
             if b.atoms_path:
-                stack = backend.build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, len(mols))
+                stack = backend.build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, nm)
             else:
                 stack = torch.stack([self.build_slices(mols[i]) for i in idx])
             dfs = [m.defocus if defocus is None else defocus[i] for i in idx]
             wp = self._propagator((n1, n2))
-            imgs = wp.image(stack, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture)
+            imgs = wp.image(stack, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture, n_batch=len(idx))
+            if to_host:
+                imgs = imgs.reshape(len(idx), n1, n2).cpu().numpy()
             for j, i in enumerate(idx):
                 out[i] = imgs[j]
         return out

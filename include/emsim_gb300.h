@@ -184,9 +184,11 @@ int emsim_gb300_make_slices_noalloc(emsim_gb300_slice_plan* plan, const float* h
  * and the extent of the shifted coordinates, in float32 exactly as numpy evaluates them.
  * coords: (n_atoms, 3) float32 device; atom_offsets: (n_mol + 1) uint32 device, molecule m
  * owning atoms [off[m], off[m + 1]) (every molecule non-empty); shift_out, space_out:
- * (n_mol, 3) float32 device. */
-int emsim_gb300_centralize(const float* coords, const uint32_t* atom_offsets, int n_mol, float* shift_out,
-                           float* space_out, void* stream);
+ * (n_mol, 3) float32 device.  When present_out != NULL (then z: (n_atoms) int32 device),
+ * present_out[4m + w] bit b is set when Z = 32w + b occurs in molecule m (Z < 128), the
+ * element set sort_elements_and_count (atoms.py:53-86) would find. */
+int emsim_gb300_centralize(const float* coords, const int32_t* z, const uint32_t* atom_offsets, int n_mol,
+                           float* shift_out, float* space_out, uint32_t* present_out, void* stream);
 
 /* emsim_gb300_build_slices for molecules given as they come (pot.build_multi_slices after
  * atoms.centralize, pipe.py:46-52): atoms in any order with their atomic numbers z
