@@ -46,6 +46,14 @@ SIGNATURES = {
     "emsim_gb300_centralize": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "emsim_gb300_build_slices_z": (_c_int, [_c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_int,
                                             _c_vp, _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_adjoint_checkpoints": (_c_int, [_c_int, _c_int]),
+    "emsim_gb300_adjoint_workspace_size": (_c_size, [_c_vp, _c_int, _c_int, _c_int, _c_ll]),
+    "emsim_gb300_multislice_image_ckpt": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_dbl, _c_dbl, _c_dbl,
+                                                   ctypes.POINTER(ctypes.c_double), _c_int, _c_dbl, _c_vp, _c_vp,
+                                                   _c_vp, _c_int, _c_int, _c_vp]),
+    "emsim_gb300_multislice_image_adjoint": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_dbl, _c_dbl, _c_dbl,
+                                                      ctypes.POINTER(ctypes.c_double), _c_int, _c_dbl, _c_vp, _c_vp,
+                                                      _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_int, _c_vp]),
 }
 
 ERROR_NAMES = {1: "invalid argument", 2: "CUDA error", 3: "unsupported", 4: "wrong device"}

@@ -19,6 +19,8 @@ enum RowOps : int {
     ROW_FFT = 4,            // forward row FFT before the store
     ROW_OUT_INTENSITY = 8,  // store |psi|^2 as float instead of complex
     ROW_CONST_IN = 16,      // input is the constant plane wave const_val (nothing is loaded)
+    ROW_STORE_PHI = 32,     // adjoint recompute: store the transmitted wave phi (after TRANSMIT)
+    ROW_GRAD = 64,          // adjoint: grad[row] = 2 sigma_grad Im(v conj(phi)) before TRANSMIT
 };
 
 struct RowArgs {
@@ -32,6 +34,11 @@ struct RowArgs {
     long long slice_img_stride = 0;
     float sigma = 0.f;
     float2 const_val = {0.f, 0.f};
+    float2* phi = nullptr;  // ROW_STORE_PHI output / ROW_GRAD input, (n1, n2) per image
+    long long phi_img_stride = 0;
+    float* grad = nullptr;  // ROW_GRAD output, (n1, n2) float per image
+    long long grad_img_stride = 0;
+    float sigma_grad = 0.f;
     int n_rows = 0;
     const float2* tw = nullptr;  // per-pass twiddle tables of the device (twiddle_table())
     int* err = nullptr;          // device error word (error_word())

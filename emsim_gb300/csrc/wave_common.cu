@@ -167,7 +167,9 @@ EMSIM_FAST_SIZES(EMSIM_DECL)
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
-    const bool tma = tma_enabled() && n2 >= 16 && ((ops & ROW_CONST_IN) || aligned16(a.in)) &&
+    // the adjoint's extra operands (ROW_STORE_PHI, ROW_GRAD) run on the one-tile-per-CTA kernel
+    const bool tma = tma_enabled() && n2 >= 16 && !(ops & (ROW_STORE_PHI | ROW_GRAD)) &&
+                     ((ops & ROW_CONST_IN) || aligned16(a.in)) &&
                      (!(ops & ROW_TRANSMIT) || (aligned16(a.slice) && (a.slice_img_stride & 3) == 0));
     if (tma) {
         switch (n2) {

@@ -54,6 +54,18 @@ __global__ void __launch_bounds__(512) row_pass_kernel(RowArgs a) {
 
     if (OPS & ROW_IFFT) fft::fft_regs<N, true, WARP_ONLY>(v, sm, b, t, addr, a.tw);
 
+    if (OPS & ROW_GRAD) {
+        // dL/dV = 2 sigma Im(mu conj(phi)) with mu = v (the back-propagated wave)
+        const float2* ph = a.phi + img * a.phi_img_stride + (long long)row * N;
+        float* g = a.grad + img * a.grad_img_stride + (long long)row * N;
+        const float s2 = 2.f * a.sigma_grad;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const float2 f = ph[t + m * T];
+            g[t + m * T] = s2 * (v[m].y * f.x - v[m].x * f.y);
+        }
+    }
+
     if (OPS & ROW_TRANSMIT) {
         const float* vs = a.slice + img * a.slice_img_stride + (long long)row * N;
 #pragma unroll
@@ -62,6 +74,12 @@ __global__ void __launch_bounds__(512) row_pass_kernel(RowArgs a) {
             sincosf(a.sigma * __ldg(vs + t + m * T), &s, &c);
             v[m] = cmul(v[m], make_float2(c, s));
         }
+    }
+
+    if (OPS & ROW_STORE_PHI) {
+        float2* ph = a.phi + img * a.phi_img_stride + (long long)row * N;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) ph[t + m * T] = v[m];
     }
 
     if (OPS & ROW_FFT) fft::fft_regs<N, false, WARP_ONLY>(v, sm, b, t, addr, a.tw);
@@ -177,6 +195,10 @@ int launch_row_n(int ops, const RowArgs& a, int n_img, cudaStream_t st) {
         EMSIM_ROW_CASE(ROW_IFFT | ROW_TRANSMIT | ROW_FFT)
         EMSIM_ROW_CASE(ROW_IFFT | ROW_OUT_INTENSITY)
         EMSIM_ROW_CASE(ROW_CONST_IN | ROW_TRANSMIT | ROW_FFT)
+        EMSIM_ROW_CASE(ROW_IFFT | ROW_TRANSMIT | ROW_FFT | ROW_STORE_PHI)
+        EMSIM_ROW_CASE(ROW_CONST_IN | ROW_TRANSMIT | ROW_FFT | ROW_STORE_PHI)
+        EMSIM_ROW_CASE(ROW_IFFT | ROW_GRAD | ROW_TRANSMIT | ROW_FFT)
+        EMSIM_ROW_CASE(ROW_IFFT | ROW_GRAD)
 #undef EMSIM_ROW_CASE
         default:
             set_error("row pass: unsupported op combination");

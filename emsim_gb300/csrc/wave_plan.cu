@@ -7,40 +7,11 @@
 // the neighbouring passes when the whole image is formed in one call.
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <vector>
 
-#include "engine.h"
+#include "wave_plan.h"
 
 using namespace emsim_gb300;
-
-namespace {
-
-constexpr int PROP_SLOTS = 64;
-
-}  // namespace
-
-struct emsim_gb300_wave_plan {
-    int n1 = 0, n2 = 0;
-    double d1 = 0, d2 = 0;
-    double wave_length = 0, gamma = 0;
-    float sigma = 0.f;           // gamma * lambda formed in FP64, rounded once
-    float dfx = 0.f, dfy = 0.f;  // 1.0f / d / n in float32 (WavePropagator.cpp:19-20)
-    double dfx64 = 0, dfy64 = 0;
-    float filter2 = 0.f;  // (0.6667f * 0.5f / max(d1, d2))^2 in float32 (WavePropagator.cpp:21-23)
-    bool fast = false;
-    int device = 0;
-    const float2* tw = nullptr;  // FFT twiddle table of the plan's device
-    int* err = nullptr;          // device error word of the plan's device
-    float2* tw1 = nullptr;  // generic path: exp(-2 pi i m / n1)
-    float2* tw2 = nullptr;
-    char* prop = nullptr;    // PROP_SLOTS x (float4 p1[n1] + float2 p2[n2]) propagator tables
-    int* cut = nullptr;      // band-limit cutoff per row (bandlimit_cutoffs)
-    double prop_dz[PROP_SLOTS];
-    int prop_used = 0;
-    int prop_next = 0;
-    std::mutex mu;
-};
 
 namespace emsim_gb300 {
 
@@ -63,10 +34,6 @@ void bandlimit_cutoffs(int n1, int n2, float dfx, float dfy, float filter2, int*
     }
 }
 
-}  // namespace emsim_gb300
-
-namespace {
-
 int check_device(const emsim_gb300_wave_plan* p) {
     EMSIM_REQUIRE(p != nullptr, EMSIM_GB300_ERR_INVALID, "null wave plan");
     int dev = -1;
@@ -76,7 +43,7 @@ int check_device(const emsim_gb300_wave_plan* p) {
 }
 
 // FP64 twiddle table exp(-2 pi i m / n) for the generic DFT.
-int make_tw(int n, float2** out) {
+static int make_tw(int n, float2** out) {
     std::vector<float2> h(n);
     for (int m = 0; m < n; ++m) {
         const double a = -2.0 * M_PI * (double)m / (double)n;
@@ -155,6 +122,10 @@ void set_lens(const emsim_gb300_wave_plan* p, ColArgs& a, double cs_mm, double a
     a.aper2 = fap * fap;
     a.lens_scale = scale;
 }
+
+}  // namespace emsim_gb300
+
+namespace {
 
 // ---- the generic (any size) path -------------------------------------------------
 int g_fft2(emsim_gb300_wave_plan* p, const float2* in, float2* out, bool inverse, int nb, cudaStream_t st) {

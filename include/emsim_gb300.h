@@ -202,6 +202,49 @@ int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* plan, const float* coords
                                const int32_t* elem_of_z, int n_batch, float* out, void* workspace,
                                size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------------
+ * Differentiation of the fused image.  No counterpart in the reference (emsim has no
+ * gradient); the forward is emsim_gb300_multislice_image (pipe.py:46-55, 79-84).
+ * Loss gradient with respect to the slice potentials by the adjoint multislice:
+ * dLoss/dV_s = 2 sigma Im(mu_s conj(phi_s)), phi_s the transmitted wave of slice s and
+ * mu_s the back-propagated adjoint wave (conjugate Fresnel step, conjugate CTF).
+ * Memory is O(sqrt(S)) waves: the forward stores the wave state every `every` slices,
+ * the adjoint recomputes one segment of `every` slices at a time.  Wave sides must be
+ * powers of two in [8, 4096] (else EMSIM_GB300_ERR_UNSUPPORTED).
+ * ------------------------------------------------------------------------------- */
+
+/* Number of checkpoint waves (each nb x n1 x n2 complex64) the checkpointed forward
+ * stores: ceil(n_slices / every) - 1. */
+int emsim_gb300_adjoint_checkpoints(int n_slices, int every);
+
+/* Bytes of 256-byte-aligned device workspace emsim_gb300_multislice_image_adjoint needs:
+ * (2 + min(every, n_slices)) waves of nb images, plus nb float images when the slices
+ * are shared (slices_stride 0) by nb > 1 images. */
+size_t emsim_gb300_adjoint_workspace_size(emsim_gb300_wave_plan* plan, int n_slices, int every, int nb,
+                                          long long slices_stride);
+
+/* emsim_gb300_multislice_image that also returns the complex image wave u (image = |u|^2)
+ * in image_wave_out (nb x n1 x n2 complex64, also the work buffer) and stores the
+ * checkpoints in ckpt (emsim_gb300_adjoint_checkpoints(n_slices, every) waves of nb
+ * images; may be NULL when that is 0).  slices_stride: 0 (one stack shared by all nb
+ * images) or the per-image stride in floats (>= n_slices * n1 * n2). */
+int emsim_gb300_multislice_image_ckpt(emsim_gb300_wave_plan* plan, const float* slices, int n_slices,
+                                      long long slices_stride, double dz, double dose, double cs_mm,
+                                      const double* defocus_host, int n_defocus, double aperture, float* image_out,
+                                      void* image_wave_out, void* ckpt, int every, int nb, void* stream);
+
+/* Adjoint: grad_image (nb x n1 x n2 float32) = dLoss/dimage -> grad_slices = dLoss/dV.
+ * Arguments as given to emsim_gb300_multislice_image_ckpt, with its image_wave and ckpt.
+ * grad_slices has the layout of slices: per image at stride slices_stride, or, for
+ * shared slices (stride 0), one (n_slices, n1, n2) stack holding the sum over the nb
+ * images taken in image order (deterministic). */
+int emsim_gb300_multislice_image_adjoint(emsim_gb300_wave_plan* plan, const float* slices, int n_slices,
+                                         long long slices_stride, double dz, double dose, double cs_mm,
+                                         const double* defocus_host, int n_defocus, double aperture,
+                                         const float* grad_image, const void* image_wave, const void* ckpt,
+                                         int every, float* grad_slices, void* workspace, size_t workspace_bytes,
+                                         int nb, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
