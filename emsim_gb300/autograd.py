@@ -1,5 +1,6 @@
 """Differentiable image formation: intensity = |lens(multislice(plane wave, slices))|^2
-with the gradient of a loss with respect to the slice potentials.
+with the gradient of a loss with respect to the slice potentials, and off-grid slices
+with the gradient with respect to the atom coordinates.
 
 emsim forms images without derivatives (pipe.py:46-55, 79-84); this module puts the
 engine's checkpointed forward (``emsim_gb300_multislice_image_ckpt``) and adjoint
@@ -20,9 +21,9 @@ import numpy as np
 import torch
 
 from . import _native
-from .backend import WavePropagator, _ptr, _stream
+from .backend import MultiSlicesBuilder, WavePropagator, _ptr, _stream
 
-__all__ = ["MultisliceImage", "image", "default_every"]
+__all__ = ["MultisliceImage", "image", "default_every", "SmoothSlices", "smooth_slices"]
 
 
 def default_every(n_slices: int) -> int:
@@ -101,3 +102,56 @@ def image(wp: WavePropagator, slices: torch.Tensor, dz: float, electron_dose: fl
     ev = int(every) if every else default_every(ns)
     return MultisliceImage.apply(slices, wp, float(dz), float(electron_dose), float(cs_mm), dfs, float(aperture), nb,
                                  ev)
+
+
+class SmoothSlices(torch.autograd.Function):
+    """Off-grid slices (``emsim_gb300_build_slices_smooth``) of molecules given as
+    coordinates sorted by element; the backward returns dLoss/dcoords (z column 0)."""
+
+    @staticmethod
+    def forward(ctx, coords: torch.Tensor, builder: MultiSlicesBuilder, counts: torch.Tensor, nb: int):
+        c = coords.detach()
+        if c.dtype != torch.float32 or not c.is_cuda:
+            raise TypeError("coords must be a float32 CUDA tensor")
+        c = c.contiguous()
+        n_atoms = int(c.shape[0])
+        plan = builder._plan.handle
+        lib = _native.load()
+        nbytes = int(lib.emsim_gb300_smooth_workspace_size(plan, n_atoms, nb))
+        ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=c.device)
+        out = torch.empty((nb, builder.n_slice, builder.n1, builder.n2), dtype=torch.float32, device=c.device)
+        _native.call("emsim_gb300_build_slices_smooth", plan, _ptr(c), n_atoms, _ptr(counts), nb, _ptr(out), _ptr(ws),
+                     nbytes, _stream())
+        ctx.save_for_backward(c, counts, out)
+        ctx.builder, ctx.nb = builder, nb
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_slices: torch.Tensor):
+        c, counts, out = ctx.saved_tensors
+        builder, nb = ctx.builder, ctx.nb
+        n_atoms = int(c.shape[0])
+        plan = builder._plan.handle
+        lib = _native.load()
+        nbytes = int(lib.emsim_gb300_smooth_workspace_size(plan, n_atoms, nb))
+        ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=c.device)
+        g = grad_slices.detach().to(torch.float32).contiguous()
+        grad = torch.zeros_like(c)
+        _native.call("emsim_gb300_build_slices_smooth_adjoint", plan, _ptr(c), n_atoms, _ptr(counts), nb, _ptr(out),
+                     _ptr(g), _ptr(grad), _ptr(ws), nbytes, _stream())
+        return grad, None, None, None
+
+
+def smooth_slices(builder: MultiSlicesBuilder, coords: torch.Tensor, elem_counts) -> torch.Tensor:
+    """Differentiable off-grid slices.  ``coords``: (N, 3) float32 CUDA tensor (columns
+    z, x, y), molecules back to back, each sorted by element; ``elem_counts``: (nE,) for
+    one molecule -> (n_slices, n1, n2), or (B, nE) -> (B, n_slices, n1, n2), counts in
+    the builder's element order."""
+    cnt = np.ascontiguousarray(np.asarray(elem_counts, dtype=np.uint32))
+    one = cnt.ndim == 1
+    cnt2 = cnt.reshape(1, -1) if one else cnt
+    if cnt2.shape[1] != len(builder.unique_elements):
+        raise ValueError(f"elem_counts must have {len(builder.unique_elements)} entries per molecule")
+    counts = torch.as_tensor(cnt2.view(np.int32), device=coords.device).contiguous()
+    out = SmoothSlices.apply(coords, builder, counts, int(cnt2.shape[0]))
+    return out[0] if one else out

@@ -9,31 +9,26 @@
 
 #include "atoms_sort.h"
 #include "binning.cuh"
+#include "slice_plan.h"
 #include "slices.h"
 
 using namespace emsim_gb300;
 
-struct emsim_gb300_slice_plan {
-    int n_elems = 0, n_slices = 0, n1 = 0, n2 = 0;
-    double dz = 0, d1 = 0, d2 = 0;
-    bool fast = false;
-    int device = 0;
-    const float2* tw = nullptr;
-    float2* tw1 = nullptr;  // generic path twiddles exp(-2 pi i m / n)
-    float2* tw2 = nullptr;
-    float* filt = nullptr;  // (n_elems, n1, n2): F(k) * SF_e(k) / N
-    int2* wq = nullptr;     // fast path: W_n2^m = exp(-2 pi i m / n2) as 2^30-scaled fixed point
-};
+namespace emsim_gb300 {
 
-namespace {
-
-int check_device(const emsim_gb300_slice_plan* p) {
+int check_slice_device(const emsim_gb300_slice_plan* p) {
     EMSIM_REQUIRE(p != nullptr, EMSIM_GB300_ERR_INVALID, "null slice plan");
     int dev = -1;
     EMSIM_CHECK_CUDA(cudaGetDevice(&dev));
     EMSIM_REQUIRE(dev == p->device, EMSIM_GB300_ERR_DEVICE, "slice plan used on a device other than its own");
     return EMSIM_GB300_OK;
 }
+
+}  // namespace emsim_gb300
+
+namespace {
+
+int check_device(const emsim_gb300_slice_plan* p) { return check_slice_device(p); }
 
 // numpy floor division (Python semantics) for the centred band-limit grid
 inline int py_floordiv(int a, int b) {

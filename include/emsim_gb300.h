@@ -203,6 +203,32 @@ int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* plan, const float* coords
                                size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------------------------
+ * Off-grid ("smooth") slices and their coordinate adjoint.  No counterpart in the
+ * reference, whose potential is piecewise constant in the atom positions because atoms
+ * are binned to pixel centres (SliceBuilder_kernel.cu:64-123).  The smooth build keeps
+ * every step of emsim_gb300_build_slices (scattering factors, band-limit round trip,
+ * clip at 1e-13, slice membership and box by the binning rule) but evaluates each atom's
+ * structure factor exp(-2 pi i k . xi / n) at its exact lateral pixel coordinate
+ * xi = (x - start) / d - 1/2 (Nyquist term cos(pi xi)); at bin centres it equals the
+ * binned build.  Arguments as emsim_gb300_build_slices; slice sides powers of two in
+ * [8, 4096].  Deterministic (fixed summation order).
+ * ------------------------------------------------------------------------------- */
+size_t emsim_gb300_smooth_workspace_size(const emsim_gb300_slice_plan* plan, unsigned n_atoms, int n_batch);
+
+/* out: (n_batch, n_slices, n1, n2) float32 smooth slices. */
+int emsim_gb300_build_slices_smooth(emsim_gb300_slice_plan* plan, const float* coords, unsigned n_atoms,
+                                    const uint32_t* elem_counts, int n_batch, float* out, void* workspace,
+                                    size_t workspace_bytes, void* stream);
+
+/* dLoss/dcoords (n_atoms, 3) float32 for dLoss/dslices = grad_slices, given the slices the
+ * smooth build returned for the same atoms.  Columns (z, x, y): z is 0 (slice membership
+ * is piecewise constant), atoms outside the box get 0. */
+int emsim_gb300_build_slices_smooth_adjoint(emsim_gb300_slice_plan* plan, const float* coords, unsigned n_atoms,
+                                            const uint32_t* elem_counts, int n_batch, const float* slices,
+                                            const float* grad_slices, float* grad_coords, void* workspace,
+                                            size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------------
  * Differentiation of the fused image.  No counterpart in the reference (emsim has no
  * gradient); the forward is emsim_gb300_multislice_image (pipe.py:46-55, 79-84).
  * Loss gradient with respect to the slice potentials by the adjoint multislice:
