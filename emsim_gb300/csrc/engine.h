@@ -65,6 +65,10 @@ struct ColArgs {
     // band-limit cutoff |k2| <= cut of row k1 as int bits), p2[k2]
     const float4* p1 = nullptr;
     const float2* p2 = nullptr;
+    // propagate: columns [live_lo, n_cols - live_hi) are outside the band-limit for every
+    // row, so their output is zero; tiles made only of such columns are written as zeros
+    // without being loaded or transformed (-1: no such columns)
+    int live_lo = -1, live_hi = -1;
     float dfx = 0.f, dfy = 0.f;  // reference float32 frequency steps
     float filter2 = 0.f;         // (0.6667 * fmax)^2 in float32
     // lens: chi = f2 * (c1 * f2 - c2) in FP64; c2 = pi * lambda * defocus, one value for

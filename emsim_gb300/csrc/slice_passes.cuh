@@ -101,8 +101,10 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     const long long npix = (long long)N * a.n2;
     const long long ld = a.n2;
     ColAddrRt addr{B};
+    // W_n2 table, padded by one entry every 16: the lookups (j * col) mod n2 of the B
+    // consecutive columns of a row have stride j, which the padding spreads over the banks
     int2* wq = reinterpret_cast<int2*>(sm + (N + N / 8) * B);
-    for (int i = threadIdx.x; i < a.n2; i += blockDim.x) wq[i] = a.wq[i];
+    for (int i = threadIdx.x; i < a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
     __syncthreads();
     const int kmask = a.n2 - 1;
     float2 acc[8];
@@ -118,14 +120,11 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
             long long re = 0, im = 0;
             for (unsigned k = lo; k < hi; ++k) {
                 const unsigned u = __ldg(a.items + k);
-                const int2 w = wq[((int)(u & 0x7fffffffu) * col) & kmask];
-                if (u >> 31) {
-                    re -= w.y;
-                    im += w.x;
-                } else {
-                    re += w.x;
-                    im += w.y;
-                }
+                const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
+                const int2 w = wq[idx + (idx >> 4)];
+                const bool odd = (u >> 31) != 0;  // second slice of the pair: times i
+                re += odd ? -w.y : w.x;
+                im += odd ? w.x : w.y;
             }
             v[m] = make_float2((float)re * 9.31322574615478515625e-10f, (float)im * 9.31322574615478515625e-10f);
         }
@@ -148,7 +147,7 @@ template <int N>
 int slice_cols_atoms_n(const SliceArgs& a, cudaStream_t st) {
     constexpr int T = N / 8;
     const int B = col_B_for(N, a.n2);
-    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)a.n2 * sizeof(int2);
+    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2);
     EMSIM_TRY(ensure_smem_attr((const void*)slice_cols_atoms_kernel<N>, smem));
     slice_cols_atoms_kernel<N><<<dim3(a.n2 / B, a.n_img * a.n_pairs), B * T, smem, st>>>(a);
     EMSIM_CHECK_LAUNCH();

@@ -131,8 +131,20 @@ __device__ __forceinline__ void propagate_col(float2 (&v)[8], int col, int t, co
     }
 }
 
+// tiles of B columns: live ones first [0, lo) and last [tiles - hi, tiles), the rest dead
+struct LiveTiles {
+    int lo, hi;
+};
+inline LiveTiles live_tiles(const ColArgs& a, int B, int tiles_per_img) {
+    if (a.live_lo < 0 || a.live_hi < 0) return {tiles_per_img, 0};
+    const int lo = (a.live_lo + B - 1) / B, hi = (a.live_hi + B - 1) / B;
+    if (lo + hi >= tiles_per_img) return {tiles_per_img, 0};
+    return {lo, hi};
+}
+
 template <int N, int MODE>
-__global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS) col_pass_kernel(ColArgs a) {
+__global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
+    col_pass_kernel(ColArgs a, int dead_lo, int dead_hi) {
     constexpr int T = N / 8;
     extern __shared__ float2 sm[];
     const int B = blockDim.x / T;
@@ -144,6 +156,12 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
 
     float2* base = a.data + img * a.img_stride + col;
     const long long ld = a.n_cols;
+    if (MODE == COL_PROPAGATE && (int)blockIdx.x >= dead_lo && (int)blockIdx.x < dead_hi) {
+        // every column of this tile lies outside the band-limit: the output is zero
+#pragma unroll
+        for (int m = 0; m < 8; ++m) base[(long long)(t + m * T) * ld] = make_float2(0.f, 0.f);
+        return;
+    }
     float2 v[8];
 #pragma unroll
     for (int m = 0; m < 8; ++m) v[m] = base[(long long)(t + m * T) * ld];
@@ -222,12 +240,15 @@ int launch_col_n(int mode, const ColArgs& a, int n_img, cudaStream_t st) {
     const int B = col_B_for(N, a.n_cols);
     const int threads = B * T;
     const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2);
-    dim3 grid(a.n_cols / B, n_img);
+    const int tiles_per_img = a.n_cols / B;
+    dim3 grid(tiles_per_img, n_img);
+    const LiveTiles lt = live_tiles(a, B, tiles_per_img);
+    const int dead_lo = lt.lo, dead_hi = tiles_per_img - lt.hi;
     switch (mode) {
 #define EMSIM_COL_CASE(MODE)                                                                                \
     case MODE: {                                                                                            \
         EMSIM_TRY(ensure_smem_attr((const void*)col_pass_kernel<N, MODE>, smem));                           \
-        col_pass_kernel<N, MODE><<<grid, threads, smem, st>>>(a);                                           \
+        col_pass_kernel<N, MODE><<<grid, threads, smem, st>>>(a, dead_lo, dead_hi);                         \
         break;                                                                                              \
     }
         EMSIM_COL_CASE(COL_PROPAGATE)

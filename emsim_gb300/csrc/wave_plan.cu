@@ -97,6 +97,9 @@ ColArgs base_col(const emsim_gb300_wave_plan* p, float2* data) {
     a.filter2 = p->filter2;
     a.dfx64 = p->dfx64;
     a.dfy64 = p->dfy64;
+    // propagation keeps |k2| <= cut_max only: columns 0..cut_max and n2-cut_max..n2-1
+    a.live_lo = p->cut_max + 1;
+    a.live_hi = p->cut_max > 0 ? p->cut_max : 0;
     return a;
 }
 
@@ -225,6 +228,7 @@ int emsim_gb300_wave_plan_create(int n1, int n2, double d1, double d2, double wa
     {
         std::vector<int> cut(n1);
         bandlimit_cutoffs(n1, n2, p->dfx, p->dfy, p->filter2, cut.data());
+        for (int i = 0; i < n1; ++i) p->cut_max = cut[i] > p->cut_max ? cut[i] : p->cut_max;
         if (cudaMemcpy(p->cut, cut.data(), sizeof(int) * n1, cudaMemcpyHostToDevice) != cudaSuccess) {
             set_error("upload of band-limit cutoffs failed");
             return fail(EMSIM_GB300_ERR_CUDA);

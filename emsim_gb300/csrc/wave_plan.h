@@ -28,6 +28,7 @@ struct emsim_gb300_wave_plan {
     float2* tw2 = nullptr;
     char* prop = nullptr;  // PROP_SLOTS x (float4 p1[n1] + float2 p2[n2]) propagator tables
     int* cut = nullptr;    // band-limit cutoff per row (bandlimit_cutoffs)
+    int cut_max = -1;      // largest cutoff over the rows: columns beyond it are dead for propagation
     double prop_dz[emsim_gb300::PROP_SLOTS];
     int prop_used = 0;
     int prop_next = 0;

@@ -144,9 +144,14 @@ struct ColTma {
     static constexpr int BOXR = N < 256 ? N : 256;  // rows per tensor copy
 };
 
+// Tiles of B columns.  The pipeline walks the live tiles only: per image the first lt_lo
+// and the last lt_hi of the tiles_per_img tiles (all of them when nothing is dead); the
+// dead tiles between them (propagate: outside the band-limit in every row) are then
+// written as zeros without being loaded.
 template <int N, int MODE>
 __global__ void __launch_bounds__(512, 2)
-    col_tma_kernel(const __grid_constant__ CUtensorMap map, ColArgs a, int B, int tiles_per_img, int n_tiles) {
+    col_tma_kernel(const __grid_constant__ CUtensorMap map, ColArgs a, int B, int tiles_per_img, int lt_lo,
+                   int lt_hi, int n_img) {
     constexpr int T = N / 8;
     constexpr int BOXR = ColTma<N>::BOXR;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -158,10 +163,19 @@ __global__ void __launch_bounds__(512, 2)
     float2* stage1 = stage0 + te;
     uint64_t* bar = reinterpret_cast<uint64_t*>(stage1 + te);
     const ColSwz addr{B, B >= 16 ? 0 : (16 / B) - 1};
+    const int live_per_img = lt_lo + lt_hi;
+    const int n_tiles = live_per_img * n_img;
+    // live tile index -> (image, column tile)
+    auto locate = [&](int tile, int& img, int& ct) {
+        img = tile / live_per_img;
+        const int j = tile - img * live_per_img;
+        ct = j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo);
+    };
 
     auto issue = [&](int tile, int buf) {
-        const int img = tile / tiles_per_img;
-        const int c0 = (tile - img * tiles_per_img) * B;
+        int img, ct;
+        locate(tile, img, ct);
+        const int c0 = ct * B;
         float2* dst = buf ? stage1 : stage0;
         tma::mbar_arrive_expect_tx(&bar[buf], te * 8u);
 #pragma unroll 1
@@ -194,8 +208,9 @@ __global__ void __launch_bounds__(512, 2)
         for (int m = 0; m < 8; ++m) v[m] = stage[(t + m * T) * B + b];
         __syncthreads();
 
-        const int img = tile / tiles_per_img;
-        const int col = (tile - img * tiles_per_img) * B + b;
+        int img, ct;
+        locate(tile, img, ct);
+        const int col = ct * B + b;
         if (MODE != COL_INV) fft::fft_regs<N, false, false>(v, stage, b, t, addr, a.tw);
         if (MODE == COL_PROPAGATE) {
             propagate_col<N>(v, col, t, a);
@@ -215,6 +230,14 @@ __global__ void __launch_bounds__(512, 2)
         tma::fence_proxy_async();
         __syncthreads();
         if (tid == 0 && tile + 2 * (int)gridDim.x < n_tiles) issue(tile + 2 * gridDim.x, buf);
+    }
+    const int dead_per_img = tiles_per_img - live_per_img;
+    for (int d = blockIdx.x; d < dead_per_img * n_img; d += gridDim.x) {
+        const int img = d / dead_per_img;
+        const int col = (lt_lo + d - img * dead_per_img) * B + b;
+        float2* base = a.data + (long long)img * a.img_stride + col;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) base[(long long)(t + m * T) * a.n_cols] = make_float2(0.f, 0.f);
     }
 }
 
@@ -277,7 +300,7 @@ int launch_col_tma_n(int mode, const ColArgs& a, int n_img, cudaStream_t st) {
     const int B = col_tma_B(N, a.n_cols);
     const int threads = B * T;
     const int tiles_per_img = a.n_cols / B;
-    const int n_tiles = tiles_per_img * n_img;
+    const LiveTiles lt = mode == COL_PROPAGATE ? live_tiles(a, B, tiles_per_img) : LiveTiles{tiles_per_img, 0};
     const size_t smem = 2 * (size_t)N * B * sizeof(float2) + 2 * sizeof(uint64_t);
     CUtensorMap map;
     EMSIM_TRY(make_col_tensor_map(&map, a.data, (long long)n_img * N, a.n_cols, B, ColTma<N>::BOXR));
@@ -286,8 +309,8 @@ int launch_col_tma_n(int mode, const ColArgs& a, int n_img, cudaStream_t st) {
     case MODE: {                                                                                 \
         const void* k = (const void*)col_tma_kernel<N, MODE>;                                    \
         EMSIM_TRY(ensure_smem_attr(k, smem));                                                    \
-        const int grid = persistent_grid(k, threads, smem, n_tiles);                             \
-        col_tma_kernel<N, MODE><<<grid, threads, smem, st>>>(map, a, B, tiles_per_img, n_tiles); \
+        const int grid = persistent_grid(k, threads, smem, tiles_per_img * n_img);               \
+        col_tma_kernel<N, MODE><<<grid, threads, smem, st>>>(map, a, B, tiles_per_img, lt.lo, lt.hi, n_img); \
         break;                                                                                   \
     }
         EMSIM_COL_TMA_CASE(COL_PROPAGATE)
