@@ -83,9 +83,9 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
 // Pass B straight from bucketed atoms (no histogram).  The row DFT of row r of slice pair
 // (img, e, pair) at column frequency k2 is z = sum over the bucket's atoms of
 // W^(j k2) (even slice) + i W^(j k2) (odd slice), W = exp(-2 pi i / n2): each term is a
-// 2^30-scaled fixed-point table entry and the sum is kept in 64-bit integers, so it is
-// exact and independent of the order in which the counting sort placed the atoms.  One
-// rounding to float32 follows.  Then, per element: forward column FFT, x T_e; over all
+// 2^22-scaled fixed-point table entry and the sum is kept in integers (32-bit for buckets
+// of up to 511 atoms, 64-bit beyond), so it is exact and independent of the order in
+// which the counting sort placed the atoms.  One rounding to float32 follows.  Then, per element: forward column FFT, x T_e; over all
 // elements: inverse column FFT -> W[img, pair].
 template <int N>
 __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS) slice_cols_atoms_kernel(SliceArgs a) {
@@ -101,11 +101,13 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     const long long npix = (long long)N * a.n2;
     const long long ld = a.n2;
     ColAddrRt addr{B};
-    // W_n2 table, padded by one entry every 16: the lookups (j * col) mod n2 of the B
-    // consecutive columns of a row have stride j, which the padding spreads over the banks
+    // W_n2 table (even slice, then times i for the odd slice), padded by one entry every
+    // 16: the lookups (j * col) mod n2 of the B consecutive columns of a row have stride j,
+    // which the padding spreads over the banks
     int2* wq = reinterpret_cast<int2*>(sm + (N + N / 8) * B);
-    for (int i = threadIdx.x; i < a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
+    for (int i = threadIdx.x; i < 2 * a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
     __syncthreads();
+    constexpr float INV_SCALE = (float)(1.0 / WQ_SCALE);
     const int kmask = a.n2 - 1;
     float2 acc[8];
 #pragma unroll
@@ -117,16 +119,28 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
         for (int m = 0; m < 8; ++m) {
             const int r = t + m * T;
             const unsigned lo = off[r], hi = off[r + 1];
-            long long re = 0, im = 0;
-            for (unsigned k = lo; k < hi; ++k) {
-                const unsigned u = __ldg(a.items + k);
-                const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
-                const int2 w = wq[idx + (idx >> 4)];
-                const bool odd = (u >> 31) != 0;  // second slice of the pair: times i
-                re += odd ? -w.y : w.x;
-                im += odd ? w.x : w.y;
+            if (hi - lo <= (unsigned)WQ_SMALL) {
+                int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
+                for (unsigned k = lo; k < hi; ++k) {
+                    const unsigned u = __ldg(a.items + k);
+                    // the odd slice of the pair reads the i W half of the table
+                    const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
+                    const int2 w = wq[idx + (idx >> 4)];
+                    re += w.x;
+                    im += w.y;
+                }
+                v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
+            } else {
+                long long re = 0, im = 0;
+                for (unsigned k = lo; k < hi; ++k) {
+                    const unsigned u = __ldg(a.items + k);
+                    const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
+                    const int2 w = wq[idx + (idx >> 4)];
+                    re += w.x;
+                    im += w.y;
+                }
+                v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
             }
-            v[m] = make_float2((float)re * 9.31322574615478515625e-10f, (float)im * 9.31322574615478515625e-10f);
         }
         fft::fft_regs<N, false, false>(v, sm, b, t, addr, a.tw);
         const float* te = a.filt + (long long)e * npix + col;
@@ -147,7 +161,7 @@ template <int N>
 int slice_cols_atoms_n(const SliceArgs& a, cudaStream_t st) {
     constexpr int T = N / 8;
     const int B = col_B_for(N, a.n2);
-    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2);
+    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(2 * a.n2 + a.n2 / 8 + 1) * sizeof(int2);
     EMSIM_TRY(ensure_smem_attr((const void*)slice_cols_atoms_kernel<N>, smem));
     slice_cols_atoms_kernel<N><<<dim3(a.n2 / B, a.n_img * a.n_pairs), B * T, smem, st>>>(a);
     EMSIM_CHECK_LAUNCH();

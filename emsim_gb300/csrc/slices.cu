@@ -310,13 +310,16 @@ int emsim_gb300_slice_plan_create(const float* sf_half, int n_elems, int n_slice
         return fail(EMSIM_GB300_ERR_CUDA);
     }
     if (p->fast) {
-        std::vector<int2> wq(n2);
+        // W^m (even slice of a pair) then i W^m (odd slice), 2^22-scaled fixed point
+        std::vector<int2> wq(2 * (size_t)n2);
         for (int m = 0; m < n2; ++m) {
             const double ang = -2.0 * M_PI * (double)m / (double)n2;
-            wq[m] = make_int2((int)std::llrint(std::cos(ang) * 1073741824.0), (int)std::llrint(std::sin(ang) * 1073741824.0));
+            const int c = (int)std::llrint(std::cos(ang) * WQ_SCALE), s = (int)std::llrint(std::sin(ang) * WQ_SCALE);
+            wq[m] = make_int2(c, s);
+            wq[n2 + m] = make_int2(-s, c);
         }
-        if (cudaMalloc((void**)&p->wq, sizeof(int2) * n2) != cudaSuccess ||
-            cudaMemcpy(p->wq, wq.data(), sizeof(int2) * n2, cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (cudaMalloc((void**)&p->wq, sizeof(int2) * 2 * n2) != cudaSuccess ||
+            cudaMemcpy(p->wq, wq.data(), sizeof(int2) * 2 * n2, cudaMemcpyHostToDevice) != cudaSuccess) {
             set_error("slice plan: fixed-point twiddle upload failed");
             return fail(EMSIM_GB300_ERR_CUDA);
         }

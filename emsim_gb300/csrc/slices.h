@@ -16,8 +16,12 @@ struct SliceArgs {
     // bucketed atoms (build from atoms)
     const unsigned* bucket_off = nullptr;  // (n_img * n_elems * n_pairs * n1 + 1) start offsets into items
     const unsigned* items = nullptr;       // (slice parity << 31) | column, grouped by bucket
-    const int2* wq = nullptr;              // W_n2^m, m < n2, as 2^30-scaled fixed point
+    const int2* wq = nullptr;              // W_n2^m then i W_n2^m, m < n2, WQ_SCALE fixed point
 };
+
+// fixed-point scale of the row-transform table: 511 entries sum below 2^31
+constexpr double WQ_SCALE = 4194304.0;  // 2^22
+constexpr int WQ_SMALL = 511;           // buckets up to this size accumulate in 32 bits
 
 // dense histogram -> slices (three passes)
 int slice_fast_build(const SliceArgs& a, cudaStream_t st);
