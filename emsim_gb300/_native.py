@@ -43,6 +43,9 @@ SIGNATURES = {
     "emsim_gb300_build_slices_workspace_size": (_c_size, [_c_vp, _c_uint, _c_int]),
     "emsim_gb300_build_slices": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
     "emsim_gb300_make_slices_noalloc": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "emsim_gb300_band_limit_workspace_size": (_c_size, [_c_int, _c_int, _c_int]),
+    "emsim_gb300_band_limit_slices": (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_add_water": (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_dbl, ctypes.c_uint64, ctypes.c_uint32, _c_vp]),
     "emsim_gb300_centralize": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "emsim_gb300_build_slices_z": (_c_int, [_c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_int,
                                             _c_vp, _c_vp, _c_size, _c_vp]),

@@ -183,20 +183,20 @@ class MultiSlicesBuilder:
         return _bin(self._plan, "emsim_gb300_bin_atoms_multi_slices", atom_coordinates_sorted_by_elems,
                     unique_elements_count, (len(self.unique_elements), self.n_slice, self.n1, self.n2))
 
-    def add_water(self, atom_histograms, generator: Optional[torch.Generator] = None):
+    def add_water(self, atom_histograms, seed: Optional[int] = None, stream_id: int = 0):
         """Voxel water (slice_builder_base.py:134-147): in voxels empty for every element,
         add Poisson(0.031 d1 d2 dz) oxygens and Poisson(2x that) hydrogens.  Z = 1 and 8
-        must be among the unique elements."""
+        must be among the unique elements.  The draws are counter-based (Philox4x32-10,
+        ``emsim_gb300_add_water``): ``seed`` reproduces them; without one a seed is drawn
+        from numpy's global generator, the generator the reference draws from."""
         h = as_device(atom_histograms, torch.float32)
-        vacs = (h == 0).all(dim=0)
-        lam = physics.water_num_dens * self.d1 * self.d2 * self.dz
-        shape = (self.n_slice, self.n1, self.n2)
-        rate = torch.full(shape, lam, dtype=torch.float32, device=h.device)
-        oxy = torch.where(vacs, torch.poisson(rate, generator=generator), torch.zeros_like(rate))
-        hyd = torch.where(vacs, torch.poisson(rate * 2, generator=generator), torch.zeros_like(rate))
         zs = list(self.unique_elements)
-        h[zs.index(1)] += hyd
-        h[zs.index(8)] += oxy
+        if 1 not in zs or 8 not in zs:
+            raise ValueError("add_water needs Z = 1 and Z = 8 among the unique elements")
+        if seed is None:
+            seed = int(np.random.randint(0, 2 ** 62, dtype=np.int64))
+        _native.call("emsim_gb300_add_water", self._plan.handle, _ptr(h), zs.index(1), zs.index(8),
+                     float(physics.water_num_dens), int(seed) & (2 ** 64 - 1), int(stream_id) & 0xFFFFFFFF, _stream())
         return _wrap(h)
 
     def make_multi_slices(self, atom_histograms, symmetric_bandlimit: bool = True):

@@ -70,8 +70,8 @@ class Pipe:
         return wp.lens_propagate(exit_wave, m.cs_mm, m.defocus, m.aperture)
 
     def run_wpo(self, mol):
-        iw = self.lens_propagate(self.get_exit_wave_wpo(mol))
-        return iw.real ** 2 + iw.imag ** 2
+        """Weak-phase image: one projected slice, transmit, lens, |psi|^2 (pipe.py:57-77)."""
+        return backend.intensity(self.lens_propagate(self.get_exit_wave_wpo(mol)))
 
     def run(self, mol):
         """Image of one molecule, (n1, n2) float32 on the device."""

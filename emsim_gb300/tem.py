@@ -1,11 +1,59 @@
-"""Microscope parameters (emsim/tem.py:36-88)."""
+"""Microscope parameters and specimen container (emsim/tem.py:9-108)."""
 from __future__ import annotations
 
 from typing import Tuple, Union
 
-from . import wave
+import torch
+
+from . import _native, wave
+from .backend import _ptr, _stream, _wrap, as_device
 from .physics import (aberration, electron_relativity_gamma, electron_wave_length_angstrom, mtf,
                       scherzer_condition)
+
+
+class Specimen:
+    """Slices (n_slices, n1, n2) with their pixel size and thickness (emsim/tem.py:9-33)."""
+
+    def __init__(self, slices, pixel_size, dz):
+        self.slices = slices
+        self.pixel_size = pixel_size
+        self.dz = dz
+
+    @property
+    def lateral_size(self):
+        return tuple(self.slices.shape[1:])
+
+    @property
+    def num_slices(self):
+        return self.slices.shape[0]
+
+    def __iter__(self):
+        self._s = 0
+        return self
+
+    def __next__(self):
+        if self._s < self.num_slices:
+            slc = self.slices[self._s, ...]
+            self._s += 1
+            return slc
+        raise StopIteration
+
+
+def band_limit_specimen(specimen: Specimen) -> Specimen:
+    """Low-pass every slice with the disc of radius 2/3 * min(n1, n2)//2 on the centred
+    frequency grid and keep the real part (emsim/tem.py:102-108), on the device
+    (``emsim_gb300_band_limit_slices``).  The reference transforms axes (0, 1) of its
+    stack, which agrees with its own (n_slices, n1, n2) layout only for cubic stacks; here
+    each slice is filtered on its lateral axes."""
+    s = as_device(specimen.slices, torch.float32)
+    if s.dim() == 2:
+        s = s[None]
+    ns, n1, n2 = (int(x) for x in s.shape)
+    out = torch.empty_like(s)
+    nbytes = int(_native.load().emsim_gb300_band_limit_workspace_size(ns, n1, n2))
+    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=s.device)
+    _native.call("emsim_gb300_band_limit_slices", _ptr(s), ns, n1, n2, _ptr(out), _ptr(ws), nbytes, _stream())
+    return Specimen(_wrap(out), specimen.pixel_size, specimen.dz)
 
 
 class TEM:

@@ -162,6 +162,26 @@ int emsim_gb300_build_slices(emsim_gb300_slice_plan* plan, const float* coords, 
                              const uint32_t* elem_counts, int n_batch, float* out, void* workspace,
                              size_t workspace_bytes, void* stream);
 
+/* Voxel water (MultiSlicesBuilderBase.add_water, emsim/backend/slice_builder_base.py:134-147,
+ * slice_builder_cuda.py:72-85): in every voxel of hist (n_elems, n_slices, n1, n2) float32
+ * that is empty for all elements, add Poisson(w) oxygens to element o_index and
+ * Poisson(2 w) hydrogens to element h_index, w = water_num_dens * d1 * d2 * dz.  The
+ * reference draws from an unseeded global generator; here voxel v draws from
+ * Philox4x32-10 with counter (v, stream_id) and key seed, so a seed reproduces the water
+ * exactly.  Needs 0 <= w <= 64. */
+int emsim_gb300_add_water(emsim_gb300_slice_plan* plan, float* hist, int h_index, int o_index,
+                          double water_num_dens, uint64_t seed, uint32_t stream_id, void* stream);
+
+/* Band-limit of a slice stack (band_limit_specimen, emsim/tem.py:102-108): every slice of
+ * slices (n_slices, n1, n2) float32 is low-passed with the disc k1^2 + k2^2 <= 4 r^2 / 9
+ * (r = min(n1, n2) // 2, k the fftfreq integers) and its real part written to out (may
+ * equal slices).  The reference transforms axes (0, 1) of the stack, which matches its
+ * own layout only for cubic stacks; here each slice is filtered on its lateral axes.
+ * n1, n2 powers of two in [8, 4096]. */
+size_t emsim_gb300_band_limit_workspace_size(int n_slices, int n1, int n2);
+int emsim_gb300_band_limit_slices(const float* slices, int n_slices, int n1, int n2, float* out, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------------------------------------------------
  * Slices without a workspace.  No counterpart in the reference.
  * For callers that cannot allocate device memory when they need slices - a plugin inside

@@ -492,6 +492,21 @@ class WavePropagator:
         return self._ifft2_unnorm(G).astype(self.cdt)
 
 
+def band_limit_slices(slices: np.ndarray) -> np.ndarray:
+    """tem.band_limit_specimen (tem.py:102-108) as intended: every (n1, n2) slice of a
+    (n_slices, n1, n2) stack is low-passed with the disc (x - n1//2)^2 + (y - n2//2)^2 <=
+    4 r^2 / 9 (r = min(n1, n2)//2) on the centred grid, ifftshifted, real part kept
+    (complex128).  The reference's own code transforms axes (0, 1) of the array it is
+    given, so it agrees with this for a stack transposed to (n1, n2, n_slices) with
+    n2 == n_slices, e.g. a cubic one."""
+    s = np.asarray(slices, dtype=np.float64)
+    n1, n2 = s.shape[-2:]
+    r = min(n1, n2) // 2
+    x, y = np.mgrid[0:n1, 0:n2]
+    fil = np.fft.ifftshift(np.where((x - n1 // 2) ** 2 + (y - n2 // 2) ** 2 <= 4 * r * r / 9, 1., 0.))
+    return np.fft.ifft2(np.fft.fft2(s, axes=(-2, -1)) * fil, axes=(-2, -1)).real
+
+
 def intensity(wave: np.ndarray) -> np.ndarray:
     """pipe.py:81-82: re^2 + im^2."""
     return wave.real ** 2 + wave.imag ** 2

@@ -5,7 +5,7 @@ resulting ``*.npz`` fixtures are committed and read by the tests everywhere else
 Every fixture stores its inputs next to the reference outputs, so no test needs the
 random generator to reproduce them.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [generator ...]
 """
 from __future__ import annotations
 
@@ -167,17 +167,27 @@ def pipes(em):
                         five_tem=np.array([tem5.defocus, tem5.aperture]))
 
 
-def main():
+def specimen(em):
+    """tem.band_limit_specimen on a cubic stack, the one shape for which the reference's
+    axes (0, 1) transform and its fil[..., None] broadcast agree (tem.py:102-108)."""
+    rng = np.random.default_rng(41)
+    x = rng.random((16, 16, 16)) * 10.0
+    out = em.tem.band_limit_specimen(em.tem.Specimen(x, 1.0, 2.0)).slices
+    np.savez_compressed(HERE / "golden_specimen.npz", cube=x, band_limited=out)
+
+
+GENERATORS = {"physics": physics, "scattering": scattering, "binning": binning, "slices": slices,
+              "waves": waves, "pipes": pipes, "specimen": specimen}
+
+
+def main(names=None):
+    """Regenerate every fixture, or only the named ones."""
     em = ref_numpy.load()
-    physics(em)
-    scattering(em)
-    binning(em)
-    slices(em)
-    waves(em)
-    pipes(em)
+    for name in names or list(GENERATORS):
+        GENERATORS[name](em)
     for f in sorted(HERE.glob("golden_*.npz")):
         print(f.name, f.stat().st_size)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

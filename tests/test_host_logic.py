@@ -164,3 +164,27 @@ def test_capi_rejects_bad_arguments_without_gpu():
 def test_native_missing_library_fails_loudly(tmp_path):
     with pytest.raises(_native.NativeUnavailable):
         _native.load(tmp_path / "nope.so")
+
+
+def test_philox_known_answers_and_water_model():
+    """Philox4x32-10 restatement against the published known-answer vectors (Random123),
+    the vectorised form against the scalar one, and the Poisson inversion's mean."""
+    import numpy as np
+
+    from oracle import water
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+           ((0xffffffff,) * 4, (0xffffffff, 0xffffffff), (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+           ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+            (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1))]
+    for c, k, want in kat:
+        assert water.philox4x32_10(c, k) == list(want)
+    v = np.array([0, 1, 7, 2 ** 33 + 5, 123456789012], dtype=np.uint64)
+    seed, stream = 0x0123456789ABCDEF, 3
+    w0, w1 = water.philox_vec(v, stream, seed)
+    for i, x in enumerate(v):
+        ref = water.philox4x32_10((int(x) & 0xFFFFFFFF, int(x) >> 32, stream, 0), (seed & 0xFFFFFFFF, seed >> 32))
+        assert (int(w0[i]), int(w1[i])) == (ref[0], ref[1])
+    words, _ = water.philox_vec(np.arange(200_000, dtype=np.uint64), 0, 99)
+    for lam in (0.062, 0.5, 3.0):
+        k = water.poisson_inv(words, lam)
+        assert abs(k.mean() - lam) < 5 * np.sqrt(lam / len(k))

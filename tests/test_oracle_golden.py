@@ -164,3 +164,13 @@ def test_freq_grid_is_fftfreq():
         fx = np.fft.fftfreq(n1, d1)
         fy = np.fft.fftfreq(n2, d2)
         np.testing.assert_allclose(f2, fx[:, None] ** 2 + fy[None, :] ** 2, rtol=1e-14)
+
+
+def test_band_limit_specimen_golden():
+    """oracle.band_limit_slices against the reference's band_limit_specimen, run on a
+    cubic stack (axes (0, 1) of the reference = the lateral axes of the transposed stack)."""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "golden_specimen.npz")
+    cube = g["cube"]
+    got = om.band_limit_slices(np.moveaxis(cube, 2, 0))
+    np.testing.assert_allclose(np.moveaxis(got, 0, 2), g["band_limited"], rtol=1e-12, atol=1e-12)
