@@ -53,6 +53,11 @@ SIGNATURES = {
     "emsim_gb300_build_slices_smooth": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
     "emsim_gb300_build_slices_smooth_adjoint": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,
                                                          _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_build_slices_ragged": (_c_int, [_c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,
+                                                 _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_multislice_image_ragged": (_c_int, [_c_vp, _c_vp, _c_ll, ctypes.POINTER(ctypes.c_int32), _c_dbl,
+                                                     _c_dbl, _c_dbl, ctypes.POINTER(ctypes.c_double), _c_int, _c_dbl,
+                                                     _c_vp, _c_vp, _c_int, _c_vp]),
     "emsim_gb300_adjoint_checkpoints": (_c_int, [_c_int, _c_int]),
     "emsim_gb300_adjoint_workspace_size": (_c_size, [_c_vp, _c_int, _c_int, _c_int, _c_ll]),
     "emsim_gb300_multislice_image_ckpt": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_dbl, _c_dbl, _c_dbl,

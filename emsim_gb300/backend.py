@@ -220,11 +220,14 @@ class MultiSlicesBuilder:
 
 def build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tensor, z: torch.Tensor,
                                    offsets: torch.Tensor, shift: torch.Tensor, mol_index: Sequence[int], n_mol: int,
-                                   symmetric_bandlimit: bool = True) -> DeviceArray:
+                                   symmetric_bandlimit: bool = True,
+                                   slot_slices: Optional[Sequence[int]] = None) -> DeviceArray:
     """Slices of molecules ``mol_index`` of a device-resident batch: ``xyz`` (n_atoms, 3)
     float32, ``z`` (n_atoms) int32, ``offsets`` (n_mol + 1) uint32 atom offsets, ``shift``
     (n_mol, 3) float32 per-molecule translation (centralisation).  Returns
-    (len(mol_index), n_slices, n1, n2) float32."""
+    (len(mol_index), n_slices, n1, n2) float32.  ``slot_slices``: each molecule's own slice
+    count (<= builder.n_slice; ragged batch): molecule k is binned on the slice axis of
+    its own count and fills slices [0, slot_slices[k]) of its stack."""
     plan = builder._plan if symmetric_bandlimit else slice_plan(
         builder.unique_elements, builder.n_slice, builder.n1, builder.n2, builder.dz, builder.d1, builder.d2,
         False)[0]
@@ -235,15 +238,26 @@ def build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tenso
     for k, zz in enumerate(sorted(int(v) for v in builder.unique_elements)):
         if 0 <= zz < 128:
             eoz[zz] = k
-    meta = torch.from_numpy(np.concatenate([slot, eoz])).to(dev, non_blocking=True)
-    n_atoms = int(xyz.shape[0])
     nb = len(mol_index)
+    parts = [slot, eoz]
+    if slot_slices is not None:
+        ss = np.asarray(slot_slices, dtype=np.int32).reshape(-1)
+        if ss.shape[0] != nb or ss.min(initial=1) < 1 or ss.max(initial=1) > builder.n_slice:
+            raise ValueError(f"slot_slices must hold {nb} counts in [1, {builder.n_slice}]")
+        parts.append(ss)
+    meta = torch.from_numpy(np.concatenate(parts)).to(dev, non_blocking=True)
+    n_atoms = int(xyz.shape[0])
     out = torch.empty((nb, builder.n_slice, builder.n1, builder.n2), dtype=torch.float32, device=dev)
     nbytes = int(_native.load().emsim_gb300_build_slices_workspace_size(plan.handle, n_atoms, nb))
     ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
-    _native.call("emsim_gb300_build_slices_z", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets), n_mol,
-                 _ptr(shift), _ptr(meta), ctypes.c_void_p(meta.data_ptr() + 4 * n_mol), nb, _ptr(out), _ptr(ws),
-                 nbytes, _stream())
+    eoz_ptr = ctypes.c_void_p(meta.data_ptr() + 4 * n_mol)
+    if slot_slices is None:
+        _native.call("emsim_gb300_build_slices_z", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets), n_mol,
+                     _ptr(shift), _ptr(meta), eoz_ptr, nb, _ptr(out), _ptr(ws), nbytes, _stream())
+    else:
+        _native.call("emsim_gb300_build_slices_ragged", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets),
+                     n_mol, _ptr(shift), _ptr(meta), eoz_ptr, ctypes.c_void_p(meta.data_ptr() + 4 * (n_mol + 128)),
+                     nb, _ptr(out), _ptr(ws), nbytes, _stream())
     return _wrap(out)
 
 
@@ -399,6 +413,37 @@ class WavePropagator:
         if return_exit_wave:
             return img, _wrap(ew[0] if squeeze else ew)
         return img
+
+
+def image_ragged(wp: "WavePropagator", stacks, n_slices: Sequence[int], dz: float, electron_dose: float,
+                 cs_mm: float, defocus, aperture: float) -> DeviceArray:
+    """Images of a ragged batch: ``stacks`` (B, S_max, n1, n2) float32 where image b uses
+    its first n_slices[b] slices.  Images are propagated longest first, each step only
+    over the images that still have a slice (``emsim_gb300_multislice_image_ragged``);
+    results come back in input order, (B, n1, n2) float32."""
+    s = as_device(stacks, torch.float32)
+    nb, smax, n1, n2 = (int(x) for x in s.shape)
+    ns = np.asarray(n_slices, dtype=np.int32).reshape(-1)
+    if ns.shape[0] != nb or ns.min(initial=1) < 1 or ns.max(initial=1) > smax:
+        raise ValueError(f"n_slices must hold {nb} counts in [1, {smax}]")
+    dfs = np.atleast_1d(np.asarray(defocus, dtype=np.float64))
+    order = np.argsort(-ns, kind="stable")
+    dev = s.device
+    if np.any(order != np.arange(nb)):
+        s = s[torch.as_tensor(order, device=dev)].contiguous()
+        dfs = np.ascontiguousarray(np.resize(dfs, nb)[order]) if dfs.size > 1 else dfs
+    ns_sorted = np.ascontiguousarray(ns[order])
+    img = torch.empty((nb, n1, n2), dtype=torch.float32, device=dev)
+    work = torch.empty((nb, n1, n2), dtype=torch.complex64, device=dev)
+    _native.call("emsim_gb300_multislice_image_ragged", wp._plan.handle, _ptr(s), smax * n1 * n2,
+                 ns_sorted.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), float(dz), float(electron_dose),
+                 float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(dfs), float(aperture),
+                 _ptr(img), _ptr(work), nb, _stream())
+    if np.any(order != np.arange(nb)):
+        inv = np.empty(nb, dtype=np.int64)
+        inv[order] = np.arange(nb)
+        img = img[torch.as_tensor(inv, device=dev)]
+    return _wrap(img)
 
 
 def intensity(wave) -> DeviceArray:

@@ -163,8 +163,17 @@ __global__ void atoms_bucket_z_kernel(AtomBucketZArgs a) {
             const float z = __fadd_rn(a.coords[3 * r + 0], sh[0]);
             const float x = __fadd_rn(a.coords[3 * r + 1], sh[1]);
             const float y = __fadd_rn(a.coords[3 * r + 2], sh[2]);
+            BinAxis az = a.ax0;
+            if (a.slot_slices) {
+                // the molecule's own slice axis, evaluated as the host's make_axis does
+                int n = a.slot_slices[slot];
+                n = n < 1 ? 1 : (n > a.ax0.n ? a.ax0.n : n);
+                az.n = n;
+                az.start = -az.d * floorf((float)(n + 1) / 2.0f);
+                az.end = fmaf((float)n, az.d, az.start);
+            }
             int s, i, j;
-            if (bin_axis(z, a.ax0, s) && bin_axis(x, a.ax1, i) && bin_axis(y, a.ax2, j)) {
+            if (bin_axis(z, az, s) && bin_axis(x, a.ax1, i) && bin_axis(y, a.ax2, j)) {
                 bk = (unsigned)((((long long)slot * a.n_elems + e) * a.n_pairs + (s >> 1)) * plane + i);
                 item = ((unsigned)(s & 1) << 31) | (unsigned)j;
                 atomicAdd(a.bucket_count + bk, 1u);

@@ -33,6 +33,9 @@ struct AtomBucketZArgs {
     const int* elem_of_z = nullptr;     // (128) element index of Z, -1 when absent
     int n_elems = 0, n_pairs = 0, n1 = 0;
     BinAxis ax0, ax1, ax2;
+    // per output image: its own slice count (<= ax0.n); the slice axis of a molecule is
+    // then the binning rule's axis for that count; nullptr: ax0 for every molecule
+    const int* slot_slices = nullptr;
     unsigned* bucket = nullptr;
     unsigned* item = nullptr;
     unsigned* bucket_count = nullptr;

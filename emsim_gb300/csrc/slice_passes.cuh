@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     const int y = blockIdx.y;  // img * n_pairs + pair
     const int img = y / a.n_pairs;
     const int pair = y - img * a.n_pairs;
+    if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
     const long long npix = (long long)N * a.n2;
     const long long ld = a.n2;
     ColAddrRt addr{B};
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(512) slice_rows_inv_kernel(SliceArgs a) {
     const int y = blockIdx.y;  // img * n_pairs + pair
     const int img = y / a.n_pairs;
     const int pair = y - img * a.n_pairs;
+    if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
     const long long npix = (long long)a.n1 * N;
     const float2* src = a.work + (long long)y * npix + (long long)row * N;
     float2 v[8];

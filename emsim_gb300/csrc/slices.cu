@@ -429,6 +429,14 @@ int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* p, const float* coords, c
                                const uint32_t* atom_offsets, int n_mol, const float* shift, const int32_t* mol_slot,
                                const int32_t* elem_of_z, int n_batch, float* out, void* workspace,
                                size_t workspace_bytes, void* stream) {
+    return emsim_gb300_build_slices_ragged(p, coords, z, n_atoms, atom_offsets, n_mol, shift, mol_slot, elem_of_z,
+                                           nullptr, n_batch, out, workspace, workspace_bytes, stream);
+}
+
+int emsim_gb300_build_slices_ragged(emsim_gb300_slice_plan* p, const float* coords, const int32_t* z,
+                                    unsigned n_atoms, const uint32_t* atom_offsets, int n_mol, const float* shift,
+                                    const int32_t* mol_slot, const int32_t* elem_of_z, const int32_t* slot_slices,
+                                    int n_batch, float* out, void* workspace, size_t workspace_bytes, void* stream) {
     EMSIM_TRY(check_device(p));
     EMSIM_REQUIRE(p->fast, EMSIM_GB300_ERR_UNSUPPORTED,
                   "build_slices_z: slice side is not a power of two in [8, 4096]; use bin_atoms + make_slices");
@@ -463,6 +471,7 @@ int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* p, const float* coords, c
     ba.ax0 = make_axis(p->n_slices, p->dz);
     ba.ax1 = make_axis(p->n1, p->d1);
     ba.ax2 = make_axis(p->n2, p->d2);
+    ba.slot_slices = slot_slices;
     ba.bucket = U(w.bucket);
     ba.item = U(w.item);
     ba.bucket_count = U(w.count);
@@ -485,6 +494,7 @@ int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* p, const float* coords, c
     a.bucket_off = U(w.off);
     a.items = U(w.items);
     a.wq = p->wq;
+    a.img_slices = slot_slices;
     return slice_atoms_build(a, st);
 }
 

@@ -17,6 +17,7 @@ struct SliceArgs {
     const unsigned* bucket_off = nullptr;  // (n_img * n_elems * n_pairs * n1 + 1) start offsets into items
     const unsigned* items = nullptr;       // (slice parity << 31) | column, grouped by bucket
     const int2* wq = nullptr;              // W_n2^m then i W_n2^m, m < n2, WQ_SCALE fixed point
+    const int* img_slices = nullptr;       // per image slice count (<= n_slices); pairs beyond are skipped
 };
 
 // fixed-point scale of the row-transform table: 511 entries sum below 2^31

@@ -472,4 +472,55 @@ int emsim_gb300_multislice_image(emsim_gb300_wave_plan* p, const float* slices, 
     return launch_row(p->n2, ROW_IFFT | ROW_OUT_INTENSITY, r, nb, st);
 }
 
+int emsim_gb300_multislice_image_ragged(emsim_gb300_wave_plan* p, const float* slices, long long slices_stride,
+                                        const int32_t* n_slices, double dz, double dose, double cs_mm,
+                                        const double* defocus, int n_defocus, double aperture, float* image_out,
+                                        void* wave_work, int nb, void* stream) {
+    EMSIM_TRY(check_device(p));
+    EMSIM_REQUIRE(p->fast, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "multislice_image_ragged: wave sides must be powers of two between 8 and 4096");
+    EMSIM_REQUIRE(slices && n_slices && image_out && wave_work && defocus && n_defocus >= 1 && nb >= 1,
+                  EMSIM_GB300_ERR_INVALID, "multislice_image_ragged: bad arguments");
+    const long long npix = (long long)p->n1 * p->n2;
+    for (int i = 0; i < nb; ++i) {
+        EMSIM_REQUIRE(n_slices[i] >= 1 && (i == 0 || n_slices[i] <= n_slices[i - 1]), EMSIM_GB300_ERR_INVALID,
+                      "multislice_image_ragged: slice counts must be >= 1 and non-increasing");
+    }
+    EMSIM_REQUIRE(nb == 1 || slices_stride >= (long long)n_slices[0] * npix, EMSIM_GB300_ERR_INVALID,
+                  "multislice_image_ragged: slices_stride below the longest stack");
+    cudaStream_t st = (cudaStream_t)stream;
+    float2* work = (float2*)wave_work;
+    const float4* p1;
+    const float2* p2;
+    EMSIM_TRY(get_prop(p, dz, st, &p1, &p2));
+    RowArgs r = base_row(p);
+    r.out = work;
+    r.slice_img_stride = slices_stride;
+    r.const_val = make_float2((float)std::sqrt(dose * p->d1 * p->d2), 0.f);
+    ColArgs c = base_col(p, work);
+    c.p1 = p1;
+    c.p2 = p2;
+    int active = nb;  // images with a slice s form a prefix of the batch
+    for (int s = 0; s < n_slices[0]; ++s) {
+        while (active > 0 && n_slices[active - 1] <= s) --active;
+        r.slice = slices + (long long)s * npix;
+        r.in = work;
+        const int ops = s == 0 ? (ROW_CONST_IN | ROW_TRANSMIT | ROW_FFT) : (ROW_IFFT | ROW_TRANSMIT | ROW_FFT);
+        EMSIM_TRY(launch_row(p->n2, ops, r, active, st));
+        EMSIM_TRY(launch_col(p->n1, COL_PROPAGATE, c, active, st));
+    }
+    for (int i0 = 0; i0 < nb; i0 += LENS_MAX) {
+        const int cnt = nb - i0 < LENS_MAX ? nb - i0 : LENS_MAX;
+        ColArgs cl = base_col(p, work + i0 * npix);
+        set_lens(p, cl, cs_mm, aperture, 1.0f / (float)p->n1);
+        cl.n_c2 = n_defocus == 1 ? 1 : cnt;
+        for (int j = 0; j < cl.n_c2; ++j) cl.c2v[j] = M_PI * p->wave_length * defocus[(i0 + j) % n_defocus];
+        EMSIM_TRY(launch_col(p->n1, COL_LENS, cl, cnt, st));
+    }
+    RowArgs ri = base_row(p);
+    ri.in = work;
+    ri.out_int = image_out;
+    return launch_row(p->n2, ROW_IFFT | ROW_OUT_INTENSITY, ri, nb, st);
+}
+
 }  // extern "C"

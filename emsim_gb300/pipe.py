@@ -18,6 +18,10 @@ from . import atoms as atm
 from . import backend, pot, tem, wave
 
 
+def _fast_len(n: int) -> bool:
+    return 8 <= n <= 4096 and (n & (n - 1)) == 0
+
+
 class Pipe:
     def __init__(self, microscope: tem.TEM, resolution: float, slice_thickness: float,
                  roi: Optional[Union[int, Tuple[int, int]]] = None, n_slices: Optional[int] = None,
@@ -106,10 +110,13 @@ class Pipe:
         The molecules travel to the device once; centralisation, element sets, binning
         and slice building run there (emsim_gb300_centralize, build_slices_z).  Only the
         per-molecule extents and element masks come back to size the slice stacks.
-        Molecules with the same stack shape share one slice-build call and one
-        image-formation call; each group uses the union of its molecules' elements (an
-        absent element adds exactly zero to a slice).  ``to_host``: return numpy images,
-        copied with one transfer per group."""
+        Molecules of one lateral size share one slice-build call and one image-formation
+        call even when their slice counts differ (a ragged batch: each molecule is binned
+        on its own slice axis, and each multislice step runs only over the images that
+        still have a slice); each group uses the union of its molecules' elements (an
+        absent element adds exactly zero to a slice), and groups of different sizes run on
+        their own CUDA streams.  ``to_host``: return numpy images, copied with one
+        transfer per group."""
         if self.add_water:
             imgs = self._run_batch_host(mols, defocus)
             return [im.get() for im in imgs] if to_host else imgs
@@ -138,25 +145,58 @@ class Pipe:
                              backend._stream())
         space_h = space.cpu().numpy()
         mask_h = present.cpu().numpy().view(np.uint32)
+        # one group per lateral size on the fused path (a ragged batch: every molecule keeps
+        # its own slice count), one per full stack shape otherwise
         groups = defaultdict(list)
+        n_sl = {}
         for i in range(nm):
-            shape = pot.finalize_slice_size(tuple(space_h[i]), (self._pixel_size, self._pixel_size),
-                                            self.slice_thickness, self.roi, None)
-            groups[shape].append(i)
+            ns, n1, n2 = pot.finalize_slice_size(tuple(space_h[i]), (self._pixel_size, self._pixel_size),
+                                                 self.slice_thickness, self.roi, None)
+            n_sl[i] = ns
+            fast = _fast_len(n1) and _fast_len(n2)
+            groups[(n1, n2) if fast else (ns, n1, n2)].append(i)
         out: List = [None] * nm
-        for (ns, n1, n2), idx in groups.items():
+        main = torch.cuda.current_stream()
+        ready = torch.cuda.Event()
+        ready.record(main)
+        side, done = [], []
+        for key, idx in groups.items():
+            n1, n2 = key[-2:]
+            idx = sorted(idx, key=lambda i: -n_sl[i])  # longest stack first
+            ss = [n_sl[i] for i in idx]
             union = np.bitwise_or.reduce(mask_h[idx], axis=0)
             uz = [32 * w + b for w in range(4) for b in range(32) if (int(union[w]) >> b) & 1]
-            b = backend.MultiSlicesBuilder(uz, ns, n1, n2, self.slice_thickness, self._pixel_size, self._pixel_size)
-            if b.atoms_path:
-                stack = backend.build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, nm)
-            else:
-                stack = torch.stack([self.build_slices(mols[i]) for i in idx])
             dfs = [m.defocus if defocus is None else defocus[i] for i in idx]
-            wp = self._propagator((n1, n2))
-            imgs = wp.image(stack, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture, n_batch=len(idx))
+            # lateral sizes overlap on the GPU: each group runs on its own stream
+            st = torch.cuda.Stream() if len(groups) > 1 else main
+            st.wait_event(ready)
+            with torch.cuda.stream(st):
+                b = backend.MultiSlicesBuilder(uz, ss[0], n1, n2, self.slice_thickness, self._pixel_size,
+                                               self._pixel_size)
+                wp = self._propagator((n1, n2))
+                ragged = ss[0] != ss[-1]
+                if b.atoms_path:
+                    stack = backend.build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, nm,
+                                                                   slot_slices=ss if ragged else None)
+                else:
+                    stack = torch.stack([self.build_slices(mols[i]) for i in idx])
+                if ragged:
+                    imgs = backend.image_ragged(wp, stack, ss, self.slice_thickness, m.electron_dose, m.cs_mm, dfs,
+                                                m.aperture)
+                else:
+                    imgs = wp.image(stack, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture,
+                                    n_batch=len(idx))
+                imgs = imgs.reshape(len(idx), n1, n2)
+                if st is not main:
+                    imgs.record_stream(main)
+            if st is not main:
+                side.append(st)
+            done.append((idx, imgs))
+        for st in side:
+            main.wait_stream(st)
+        for idx, imgs in done:
             if to_host:
-                imgs = imgs.reshape(len(idx), n1, n2).cpu().numpy()
+                imgs = imgs.cpu().numpy()  # one transfer per group
             for j, i in enumerate(idx):
                 out[i] = imgs[j]
         return out

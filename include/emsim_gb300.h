@@ -291,6 +291,33 @@ int emsim_gb300_multislice_image_adjoint(emsim_gb300_wave_plan* plan, const floa
                                          int every, float* grad_slices, void* workspace, size_t workspace_bytes,
                                          int nb, void* stream);
 
+/* ---------------------------------------------------------------------------------
+ * Ragged batches: molecules of one lateral size with different slice counts in one call.
+ * No counterpart in the reference, which builds and propagates one molecule at a time
+ * (pipe.py:46-55, simulator.py:71-91).
+ * ------------------------------------------------------------------------------- */
+
+/* emsim_gb300_build_slices_z with a slice count per output image: slot_slices (n_batch)
+ * int32 device, each in [1, plan n_slices].  Molecule m is binned along z with the
+ * binning rule's axis for slot_slices[mol_slot[m]] slices (the axis pot.build_multi_slices
+ * would use for that molecule alone) and its stack fills slices [0, slot_slices[slot]) of
+ * its (n_slices, n1, n2) slot; the slices beyond are not computed and hold no defined
+ * values. */
+int emsim_gb300_build_slices_ragged(emsim_gb300_slice_plan* plan, const float* coords, const int32_t* z,
+                                    unsigned n_atoms, const uint32_t* atom_offsets, int n_mol, const float* shift,
+                                    const int32_t* mol_slot, const int32_t* elem_of_z, const int32_t* slot_slices,
+                                    int n_batch, float* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* emsim_gb300_multislice_image for nb images with their own slice counts
+ * n_slices_host[i] >= 1, given in non-increasing order (sort the batch by slice count):
+ * step s propagates only the images that still have a slice s, so no step is spent on
+ * padding.  Image i reads its slice s at slices + i * slices_stride + s * n1 * n2
+ * (slices_stride >= n_slices_host[0] * n1 * n2).  Wave sides powers of two in [8, 4096]. */
+int emsim_gb300_multislice_image_ragged(emsim_gb300_wave_plan* plan, const float* slices, long long slices_stride,
+                                        const int32_t* n_slices_host, double dz, double dose, double cs_mm,
+                                        const double* defocus_host, int n_defocus, double aperture,
+                                        float* image_out, void* wave_work, int nb, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
