@@ -198,6 +198,12 @@ def run_ours(args):
 
     B = args.batch
     seeds = [1000 * rank + i for i in range(B)]
+    # pass kernels and tiles picked by the autotuner for the sizes measured below
+    from emsim_gb300 import autotune
+    tuned = {}
+    if not args.no_tune:
+        for n, nb in [(WORKLOAD["roi"], B), (512, 32), (2048, 2)]:
+            tuned[f"{n}x{n}"] = autotune.tune(n, n, batch=nb, n_slices=6, reps=3, store=False)
     db = DeviceBatch(seeds, torch, backend, atoms, pot)
     dev = torch.device("cuda", local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -312,7 +318,8 @@ def run_ours(args):
         "config": {"workload": "blob 50k C/N/O/S atoms r=40A, roi 256, pixel 1A, dz 2A, %d slices, 200 keV, "
                                "Cs 1.3 mm, df 700 A, aperture 10 mrad" % db.ns,
                    "images_per_step_per_gpu": B, "l2": "flushed (256 MiB write) before every timed step",
-                   "cuda_graph": graph is not None, "parallelism": f"image-parallel x{world}"},
+                   "cuda_graph": graph is not None, "parallelism": f"image-parallel x{world}",
+                   "autotune": {k: {"row": v["row"], "col": v["col"]} for k, v in tuned.items()}},
         "slice_steps_per_s": round(value * db.ns, 1),
         "slice_step_throughput": {str(k): {"slice_steps_per_s": round(v["slice_steps_per_s"], 1),
                                            "hbm_frac": round(v["frac"], 4), "images": v["images"]}
@@ -421,6 +428,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -88,6 +88,19 @@ inline bool fast_len(int n) { return n >= 8 && n <= 4096 && (n & (n - 1)) == 0; 
 int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st);
 int launch_col(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st);
 
+// Per-length tuning of the two passes (emsim_gb300_set_pass_tuning): use the TMA kernel
+// (-1: when it applies, 0: never) and the rows / columns per tile (0: built-in).  Tiles
+// only regroup independent rows or columns, so results do not depend on the tuning.
+struct PassTuning {
+    int row_tma = -1, row_rows = 0, col_tma = -1, col_cols = 0;
+};
+PassTuning pass_tuning(int n);
+// the tile a launcher uses: hint when it is a power of two in [min_tile, def), else def
+inline int tile_with_hint(int def, int hint, int min_tile) {
+    if (hint >= min_tile && hint < def && (hint & (hint - 1)) == 0) return hint;
+    return def;
+}
+
 // row-pass geometry actually used (rows per CTA) - exposed for tests and the autotuner
 int row_tile(int n2);
 int col_tile(int n1);

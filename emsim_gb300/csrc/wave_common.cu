@@ -166,9 +166,25 @@ EMSIM_FAST_SIZES(EMSIM_DECL)
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
+// tuning table indexed by log2(n), n = 8 .. 4096
+PassTuning g_tuning[13];
+std::mutex g_tuning_mu;
+
+static int log2_fast(int n) {
+    int k = 0;
+    while ((1 << k) < n) ++k;
+    return k;
+}
+
+PassTuning pass_tuning(int n) {
+    if (!fast_len(n)) return PassTuning{};
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    return g_tuning[log2_fast(n)];
+}
+
 int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
     // the adjoint's extra operands (ROW_STORE_PHI, ROW_GRAD) run on the one-tile-per-CTA kernel
-    const bool tma = tma_enabled() && n2 >= 16 && !(ops & (ROW_STORE_PHI | ROW_GRAD)) &&
+    const bool tma = tma_enabled() && n2 >= 16 && pass_tuning(n2).row_tma != 0 && !(ops & (ROW_STORE_PHI | ROW_GRAD)) &&
                      ((ops & ROW_CONST_IN) || aligned16(a.in)) &&
                      (!(ops & ROW_TRANSMIT) || (aligned16(a.slice) && (a.slice_img_stride & 3) == 0));
     if (tma) {
@@ -190,7 +206,8 @@ int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
 }
 
 int launch_col(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st) {
-    const bool tma = tma_enabled() && n1 >= 16 && col_tma_B(n1, a.n_cols) >= 2 && aligned16(a.data);
+    const bool tma = tma_enabled() && n1 >= 16 && pass_tuning(n1).col_tma != 0 && col_tma_B(n1, a.n_cols) >= 2 &&
+                     aligned16(a.data);
     if (tma) {
         switch (n1) {
 #define EMSIM_CASE(N) \
@@ -426,3 +443,33 @@ extern "C" int emsim_gb300_check_device_error(int* code) {
     return EMSIM_GB300_OK;
 }
 extern "C" int emsim_gb300_abi_version(void) { return EMSIM_GB300_ABI_VERSION; }
+
+extern "C" int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int col_tma, int col_cols) {
+    using namespace emsim_gb300;
+    EMSIM_REQUIRE(fast_len(n), EMSIM_GB300_ERR_INVALID, "set_pass_tuning: n must be a power of two in [8, 4096]");
+    EMSIM_REQUIRE(row_tma >= -1 && row_tma <= 1 && col_tma >= -1 && col_tma <= 1 && row_rows >= 0 && col_cols >= 0,
+                  EMSIM_GB300_ERR_INVALID, "set_pass_tuning: tma flags in {-1, 0, 1}, tiles >= 0");
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    PassTuning& t = g_tuning[log2_fast(n)];
+    t.row_tma = row_tma == 1 ? -1 : row_tma;
+    t.row_rows = row_rows;
+    t.col_tma = col_tma == 1 ? -1 : col_tma;
+    t.col_cols = col_cols;
+    return EMSIM_GB300_OK;
+}
+
+extern "C" int emsim_gb300_get_pass_tuning(int n, int* out) {
+    using namespace emsim_gb300;
+    EMSIM_REQUIRE(fast_len(n) && out, EMSIM_GB300_ERR_INVALID, "get_pass_tuning: bad arguments");
+    const PassTuning t = pass_tuning(n);
+    out[0] = t.row_tma;
+    out[1] = t.row_rows;
+    out[2] = t.col_tma;
+    out[3] = t.col_cols;
+    // the tiles the launchers would use without hints (TMA row, simple row, TMA column, simple column)
+    out[4] = n >= 16 ? (n / 8 > 256 ? n / 8 : 256) / (n / 8) : 0;
+    out[5] = row_threads(n) / (n / 8);
+    out[6] = col_tma_B(n, n);
+    out[7] = col_B_for(n, n);
+    return EMSIM_GB300_OK;
+}

@@ -195,7 +195,7 @@ template <int N>
 int launch_row_n(int ops, const RowArgs& a, int n_img, cudaStream_t st) {
     constexpr int T = N / 8;
     int threads = row_threads(N);
-    int B = threads / T;
+    int B = tile_with_hint(threads / T, pass_tuning(N).row_rows, 1);
     if (B > a.n_rows) B = a.n_rows;
     threads = B * T;
     const size_t smem = (size_t)fft::RowLayout<N>::words(B) * sizeof(float2);
@@ -237,7 +237,7 @@ inline int col_B_for(int n, int n_cols) {
 template <int N>
 int launch_col_n(int mode, const ColArgs& a, int n_img, cudaStream_t st) {
     constexpr int T = N / 8;
-    const int B = col_B_for(N, a.n_cols);
+    const int B = tile_with_hint(col_B_for(N, a.n_cols), pass_tuning(N).col_cols, 1);
     const int threads = B * T;
     const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2);
     const int tiles_per_img = a.n_cols / B;

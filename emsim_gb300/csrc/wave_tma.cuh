@@ -255,7 +255,7 @@ bool tma_enabled();
 template <int N>
 int launch_row_tma_n(int ops, const RowArgs& a, int n_img, cudaStream_t st) {
     constexpr int T = N / 8;
-    int B = RowTma<N>::THREADS / T;
+    int B = tile_with_hint(RowTma<N>::THREADS / T, pass_tuning(N).row_rows, 1);
     if (B > a.n_rows) B = a.n_rows;
     const int threads = B * T;
     const int tiles_per_img = a.n_rows / B;
@@ -297,7 +297,7 @@ inline int col_tma_B(int n, int n_cols) {
 template <int N>
 int launch_col_tma_n(int mode, const ColArgs& a, int n_img, cudaStream_t st) {
     constexpr int T = N / 8;
-    const int B = col_tma_B(N, a.n_cols);
+    const int B = tile_with_hint(col_tma_B(N, a.n_cols), pass_tuning(N).col_cols, 2);
     const int threads = B * T;
     const int tiles_per_img = a.n_cols / B;
     const LiveTiles lt = mode == COL_PROPAGATE ? live_tiles(a, B, tiles_per_img) : LiveTiles{tiles_per_img, 0};

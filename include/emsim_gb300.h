@@ -292,6 +292,20 @@ int emsim_gb300_multislice_image_adjoint(emsim_gb300_wave_plan* plan, const floa
                                          int nb, void* stream);
 
 /* ---------------------------------------------------------------------------------
+ * Pass tuning (no counterpart in the reference, whose FFTs are cuFFT / FFTW plans).
+ * For wave passes of length n (power of two in [8, 4096]): whether the TMA-staged
+ * persistent kernel may run (row_tma / col_tma: -1 or 1 = when it applies, 0 = never) and
+ * the rows / columns per tile (0 = built-in; a smaller power of two is honoured).  Tiles
+ * regroup independent rows or columns only, so results are identical for every setting.
+ * The table is process-wide; emsim_gb300.autotune measures candidates and caches the
+ * choice per GPU and size.
+ * ------------------------------------------------------------------------------- */
+int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int col_tma, int col_cols);
+/* out[0..3]: the current setting; out[4..7]: built-in tiles of the TMA row, simple row,
+ * TMA column and simple column kernels for an n x n wave. */
+int emsim_gb300_get_pass_tuning(int n, int* out);
+
+/* ---------------------------------------------------------------------------------
  * Ragged batches: molecules of one lateral size with different slice counts in one call.
  * No counterpart in the reference, which builds and propagates one molecule at a time
  * (pipe.py:46-55, simulator.py:71-91).

@@ -188,3 +188,22 @@ def test_philox_known_answers_and_water_model():
     for lam in (0.062, 0.5, 3.0):
         k = water.poisson_inv(words, lam)
         assert abs(k.mean() - lam) < 5 * np.sqrt(lam / len(k))
+
+
+def test_pass_tuning_table_host_side():
+    """emsim_gb300_set/get_pass_tuning validate and store without touching a GPU."""
+    import ctypes
+
+    from emsim_gb300 import _native
+    lib = _native.load()
+    out = (ctypes.c_int * 8)()
+    assert lib.emsim_gb300_get_pass_tuning(256, out) == 0
+    assert list(out)[:4] == [-1, 0, -1, 0]
+    assert list(out)[4:] == [8, 8, 16, 16]  # built-in tiles at 256: 256 threads / 32 per row, 512 / 32 columns
+    assert lib.emsim_gb300_set_pass_tuning(256, 0, 4, 1, 8) == 0
+    lib.emsim_gb300_get_pass_tuning(256, out)
+    assert list(out)[:4] == [0, 4, -1, 8]
+    assert lib.emsim_gb300_set_pass_tuning(256, -1, 0, -1, 0) == 0
+    assert lib.emsim_gb300_set_pass_tuning(100, -1, 0, -1, 0) == 1  # not a power of two
+    assert lib.emsim_gb300_set_pass_tuning(256, 2, 0, -1, 0) == 1
+    assert lib.emsim_gb300_set_pass_tuning(256, -1, -3, -1, 0) == 1
