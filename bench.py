@@ -37,7 +37,7 @@ METRIC = "images/s (50k-atom blob, 256^2, 40 slices, plain FP32)"
 
 
 def blob(seed: int):
-    from oracle.multislice import protein_blob  # seeded synthetic input generator
+    from emsim_gb300.synth import protein_blob  # seeded synthetic input generator
     return protein_blob(WORKLOAD["n_atoms"], WORKLOAD["radius"], seed)
 
 
@@ -184,6 +184,68 @@ def slice_step_roofline(torch, backend, n: int, n_img: int, n_slices: int, peak_
             "frac": algo / per_step / 1e9 / peak_gbs}
 
 
+def differentiation_extra(torch, reps: int = 3) -> dict:
+    """Forward + backward of the differentiation workload: 20,000 C/N/O/S atoms in a 50 A
+    ball, 512 x 512 at 0.5 A, 64 slices of 1 A, 32 defocus values, MSE against the image
+    of a copy jittered by 0.2 A; gradients with respect to the atom coordinates (off-grid
+    slices) and the slices (adjoint multislice, sqrt(N) checkpoints)."""
+    from emsim_gb300 import atoms, autograd, backend, synth
+    el, xyz0 = synth.protein_blob(20_000, 50.0, 77)
+    mol, uz, cnt = atoms.sort_elements_and_count(atoms.AtomList(el, xyz0))
+    rng = np.random.default_rng(78)
+    xyz = mol.coordinates
+    jit = (xyz + rng.normal(scale=0.2, size=xyz.shape)).astype(np.float32)
+    dfs = list(rng.uniform(300.0, 1500.0, size=32))
+    b = backend.MultiSlicesBuilder(list(uz), 64, 512, 512, 1.0, 0.5, 0.5)
+    wp = backend.WavePropagator(512, 512, 0.5, 0.5, 200.0)
+    with torch.no_grad():
+        target = autograd.image(wp, autograd.smooth_slices(b, torch.tensor(jit, device="cuda"), cnt), 1.0, 20.0, 1.3,
+                                dfs, 10e-3)
+    c = torch.tensor(xyz, device="cuda", requires_grad=True)
+    tf, tb = [], []
+    for it in range(reps + 2):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        img = autograd.image(wp, autograd.smooth_slices(b, c, cnt), 1.0, 20.0, 1.3, dfs, 10e-3)
+        loss = torch.mean((img - target) ** 2)
+        e1.record()
+        loss.backward()
+        e2.record()
+        e2.synchronize()
+        c.grad = None
+        if it >= 2:
+            tf.append(e0.elapsed_time(e1))
+            tb.append(e1.elapsed_time(e2))
+    f, bw = float(np.median(tf)), float(np.median(tb))
+    return {"workload": "20k C/N/O/S atoms r=50A, 512^2 at 0.5A, 64 slices of 1A, 32 defocus 300-1500A, 200 keV, "
+                        "MSE vs 0.2A-jittered copy; dLoss/dxyz and dLoss/dV",
+            "images_per_s": round(32 / ((f + bw) * 1e-3), 1), "forward_ms": round(f, 3), "backward_ms": round(bw, 3),
+            "checkpoint_every": autograd.default_every(64)}
+
+
+def batching_extra(torch, p, n_blobs: int = 32, reps: int = 2) -> dict:
+    """A mixed batch through Pipe.run_batch: blobs with log-uniform 5k-200k atoms at
+    0.1 A^-3, random orientations, roi 256 or 512, every other one in amorphous ice;
+    wall clock from host atoms to device images (ragged slice counts, two lateral sizes
+    on two streams)."""
+    from emsim_gb300 import atoms, synth
+    mix = synth.batching_mix(n_blobs, seed=11, pixel=0.5 * WORKLOAD["resolution"])
+    mols = [atoms.AtomList(el, xyz) for el, xyz, _ in mix]
+    rois = [r for _, _, r in mix]
+    p.run_batch(mols, rois=rois)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        p.run_batch(mols, rois=rois)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    return {"workload": f"{n_blobs} blobs of the batching mix (5k-200k atoms log-uniform, 0.1 A^-3, random "
+                        f"orientation, roi 256/512, half in ice), pixel 1 A, dz 2 A, one Pipe.run_batch call",
+            "images_per_s": round(n_blobs / dt, 1), "seconds_per_batch": round(dt, 4),
+            "atoms": int(sum(len(m.elements) for m in mols)), "roi_256": rois.count(256), "roi_512": rois.count(512),
+            "timing": "wall clock from host AtomLists to device images (H2D included)"}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -283,15 +345,9 @@ def run_ours(args):
             dist.destroy_process_group()
         return
 
-    # ---- accuracy of the benched image vs the FP64 oracle (outside timing) ----------
-    from oracle import multislice as om
-    el, xyz = blob(seeds[0])
-    ref64 = om.pipe_run(el, xyz, resolution=W["resolution"], slice_thickness=W["slice_thickness"], roi=W["roi"],
-                        beam_energy_kev=W["kev"], dose=W["dose"], cs_mm=W["cs_mm"], defocus=W["defocus"],
-                        aperture=W["aperture"], semantics="fftw", dtype=np.float64)
     img0 = db.img[0].cpu().numpy()
-    acc = {"rel_l2_image_vs_fp64": om.rel_l2(img0, ref64),
-           "rel_l2_contrast_vs_fp64": om.rel_l2(img0 - img0.mean(), ref64 - ref64.mean())}
+    diff = differentiation_extra(torch)
+    batching = batching_extra(torch, p)
 
     # ---- roofline of the dominant kernel pair (slice step) ----------------------
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
@@ -307,8 +363,9 @@ def run_ours(args):
                 "frac": round(main["frac"], 4), "traffic": traffic.get("slice_step_256"),
                 "peak_source": peak_src, "algorithmic_bytes_per_launch": 20 * 256 * 256 * B}
 
-    # ---- CPU baseline: the oracle's restatement of the reference numpy path ------
-    cpu = cpu_baseline(budget_s=args.cpu_seconds)
+    # ---- CPU baseline: the oracle's restatement of the reference numpy path, and the
+    # checker's FP64 image of the first benched blob ------------------------------
+    cpu, acc = cpu_baseline(budget_s=args.cpu_seconds, check=(seeds[0], img0))
 
     clocks = clk.summary()
     out = {
@@ -325,6 +382,8 @@ def run_ours(args):
                                            "hbm_frac": round(v["frac"], 4), "images": v["images"]}
                                   for k, v in rl.items()},
         "accuracy": acc,
+        "differentiation": diff,
+        "batching": batching,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -367,8 +426,10 @@ def _cpu_one(seed: int) -> float:
     return time.perf_counter() - t0
 
 
-def cpu_baseline(budget_s: float = 15.0, processes: int = 1):
-    """Images/s of the reference numpy algorithm on host cores (bounded sample)."""
+def cpu_baseline(budget_s: float = 15.0, processes: int = 1, check=None):
+    """Images/s of the reference numpy algorithm on host cores (bounded sample).  With
+    ``check`` = (seed, GPU image), also the relative L2 error of that image against the
+    FP64 oracle (outside the timed sample); returns (baseline, accuracy) then."""
     import multiprocessing as mp
     t0 = time.perf_counter()
     n = 0
@@ -388,10 +449,22 @@ def cpu_baseline(budget_s: float = 15.0, processes: int = 1):
                 rounds += 1
             dt = time.perf_counter() - t0
             n = rounds * processes
-    return {"value": round(n / dt, 4), "unit": "images/s", "cores": processes, "kind": "port",
+    base = {"value": round(n / dt, 4), "unit": "images/s", "cores": processes, "kind": "port",
             "sample": f"{n} image(s) of the bench workload through the reference numpy algorithm "
                       f"(oracle 'numpy' semantics, bit-exact with emsim's numpy backend, complex128, "
                       f"numpy FFT) in {dt:.1f} s"}
+    if check is None:
+        return base
+    from oracle import multislice as om
+    W = WORKLOAD
+    seed, img = check
+    el, xyz = blob(seed)
+    ref64 = om.pipe_run(el, xyz, resolution=W["resolution"], slice_thickness=W["slice_thickness"], roi=W["roi"],
+                        beam_energy_kev=W["kev"], dose=W["dose"], cs_mm=W["cs_mm"], defocus=W["defocus"],
+                        aperture=W["aperture"], semantics="fftw", dtype=np.float64)
+    acc = {"rel_l2_image_vs_fp64": om.rel_l2(img, ref64),
+           "rel_l2_contrast_vs_fp64": om.rel_l2(img - img.mean(), ref64 - ref64.mean())}
+    return base, acc
 
 
 def run_reference(args):

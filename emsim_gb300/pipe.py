@@ -104,7 +104,7 @@ class Pipe:
         return self._pin_xyz[:n_atoms], self._pin_z[:n_atoms]
 
     def run_batch(self, mols: Sequence[atm.AtomList], defocus: Optional[Sequence[float]] = None,
-                  to_host: bool = False) -> List:
+                  to_host: bool = False, rois: Optional[Sequence] = None) -> List:
         """Images of many molecules (optionally one defocus each), in input order.
 
         The molecules travel to the device once; centralisation, element sets, binning
@@ -116,7 +116,8 @@ class Pipe:
         still have a slice); each group uses the union of its molecules' elements (an
         absent element adds exactly zero to a slice), and groups of different sizes run on
         their own CUDA streams.  ``to_host``: return numpy images, copied with one
-        transfer per group."""
+        transfer per group.  ``rois``: a lateral size (int or (n1, n2)) per molecule in
+        place of the pipe's roi."""
         if self.add_water:
             imgs = self._run_batch_host(mols, defocus)
             return [im.get() for im in imgs] if to_host else imgs
@@ -150,8 +151,10 @@ class Pipe:
         groups = defaultdict(list)
         n_sl = {}
         for i in range(nm):
+            lateral = self.roi if rois is None else (
+                (rois[i], rois[i]) if isinstance(rois[i], (int, np.integer)) else tuple(rois[i]))
             ns, n1, n2 = pot.finalize_slice_size(tuple(space_h[i]), (self._pixel_size, self._pixel_size),
-                                                 self.slice_thickness, self.roi, None)
+                                                 self.slice_thickness, lateral, None)
             n_sl[i] = ns
             fast = _fast_len(n1) and _fast_len(n2)
             groups[(n1, n2) if fast else (ns, n1, n2)].append(i)

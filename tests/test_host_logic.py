@@ -207,3 +207,18 @@ def test_pass_tuning_table_host_side():
     assert lib.emsim_gb300_set_pass_tuning(100, -1, 0, -1, 0) == 1  # not a power of two
     assert lib.emsim_gb300_set_pass_tuning(256, 2, 0, -1, 0) == 1
     assert lib.emsim_gb300_set_pass_tuning(256, -1, -3, -1, 0) == 1
+
+
+def test_synthetic_blob_matches_oracle_generator():
+    """The package's seeded blob generator (used by the benchmark) reproduces the one the
+    tests use, so benchmark inputs and parity inputs are the same atoms."""
+    import numpy as np
+
+    from emsim_gb300 import synth
+    from oracle import multislice as om
+    a, b = synth.protein_blob(3000, 15.0, 9), om.protein_blob(3000, 15.0, 9)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    mix = synth.batching_mix(4, seed=2)
+    assert len(mix) == 4 and {r for _, _, r in mix} <= {256, 512}
+    assert all(set(np.unique(el)) <= {1, 6, 7, 8, 16} for el, _, _ in mix)
+    assert np.any(mix[1][0] == 1) and not np.any(mix[0][0] == 1)  # odd blobs carry ice
