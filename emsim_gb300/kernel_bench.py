@@ -26,13 +26,17 @@ from . import _native, backend
 
 
 def _time(fn, reps: int, flush: torch.Tensor) -> float:
+    """Median seconds per call; the timed calls sit in the NVTX range "timed" so that a
+    profiler can capture exactly them."""
     ts = []
     for _ in range(reps):
         flush.fill_(1.0)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("timed")
         e0.record()
         fn()
         e1.record()
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1) * 1e-3)
     return float(np.median(ts))
@@ -48,6 +52,8 @@ def main(argv=None):
     ap.add_argument("--atoms", type=int, default=50000)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--autotune", action="store_true", help="tune the pass kernels for --n first")
+    ap.add_argument("--tuning-from-cache", action="store_true", help="apply the cached tuning for --n")
     args = ap.parse_args(argv)
     dev = torch.device("cuda", torch.cuda.current_device())
     torch.manual_seed(0)
@@ -56,6 +62,11 @@ def main(argv=None):
     st = lambda: ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)  # noqa: E731
     P = backend._ptr
     out = {"case": args.case, "n": n}
+    if args.autotune or args.tuning_from_cache:
+        from . import autotune
+        out["tuning"] = autotune.ensure(n, n) if args.tuning_from_cache else autotune.tune(n, n, batch=B)
+        if out["tuning"] is None:
+            raise SystemExit(f"no cached tuning for {n}x{n} in {autotune.cache_path()}")
     if args.case in ("step", "space", "lens", "image"):
         wp = backend.WavePropagator(n, n, 0.5, 0.5, 200.0)
         w = torch.ones((B, n, n), dtype=torch.complex64, device=dev)
