@@ -53,6 +53,8 @@ SIGNATURES = {
     "emsim_gb300_build_slices_smooth": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
     "emsim_gb300_build_slices_smooth_adjoint": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,
                                                          _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_set_precision": (_c_int, [_c_int]),
+    "emsim_gb300_get_precision": (_c_int, []),
     "emsim_gb300_set_pass_tuning": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_int]),
     "emsim_gb300_get_pass_tuning": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_int)]),
     "emsim_gb300_build_slices_ragged": (_c_int, [_c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,

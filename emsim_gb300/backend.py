@@ -446,6 +446,23 @@ def image_ragged(wp: "WavePropagator", stacks, n_slices: Sequence[int], dz: floa
     return _wrap(img)
 
 
+PRECISIONS = {"fp32": 0, "bf16x3": 1}
+
+
+def set_precision(mode: str) -> None:
+    """Precision of the wave passes, process-wide: "fp32" (plain FP32 Stockham FFTs, the
+    default) or "bf16x3" (256-point rows and columns of the multislice step on the tensor
+    cores as split-BF16 DFT GEMMs with fp32 accumulation; other sizes stay FP32)."""
+    if mode not in PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+    _native.call("emsim_gb300_set_precision", PRECISIONS[mode])
+
+
+def get_precision() -> str:
+    v = int(_native.load().emsim_gb300_get_precision())
+    return {k: m for m, k in PRECISIONS.items()}[v]
+
+
 def intensity(wave) -> DeviceArray:
     """|psi|^2 of a complex64 array through the engine."""
     w = as_device(wave, torch.complex64)

@@ -95,6 +95,13 @@ struct PassTuning {
     int row_tma = -1, row_rows = 0, col_tma = -1, col_cols = 0;
 };
 PassTuning pass_tuning(int n);
+
+// Split-BF16 tensor-core passes (wave_bf16.cu), used when the precision mode is 1 and the
+// call has their shape (length 256; row IFFT|TRANSMIT|FFT, column PROPAGATE).  They
+// return false when they do not apply, else launch and put the status in *status.
+int precision_mode();
+bool launch_row_bf16(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st, int* status);
+bool launch_col_bf16(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st, int* status);
 // the tile a launcher uses: hint when it is a power of two in [min_tile, def), else def
 inline int tile_with_hint(int def, int hint, int min_tile) {
     if (hint >= min_tile && hint < def && (hint & (hint - 1)) == 0) return hint;

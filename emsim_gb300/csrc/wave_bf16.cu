@@ -1,0 +1,341 @@
+// Split-BF16 tensor-core passes for 256-point transforms (the precision form of the
+// multislice step).
+//
+// A 256-point DFT is two batched 16-point DFTs with a twiddle between them (four-step
+// FFT, 256 = 16 x 16): for x[n1 + 16 n2],
+//     Y[n1][k2] = sum_n2 x[n1 + 16 n2] W16^(n2 k2),   Y *= W256^(n1 k2),
+//     X[k2 + 16 k1] = sum_n1 Y[n1][k2] W16^(n1 k1).
+// Each 16-point stage over a tile of R = 8 vectors is one GEMM on the 5th-generation
+// tensor cores: A = 128 rows (vector, index) x K = 32 (re/im of the 16 inputs), B = the
+// 32 x 32 real form of the complex DFT matrix, D = 128 x 32 fp32 in tensor memory.  The
+// operands are split into bf16 hi + lo parts (x = hi + lo, lo = bf16(x - hi)) and
+// D = A_hi B_hi + A_hi B_lo + A_lo B_hi, accumulated in fp32 (the lo x lo term is below
+// the bf16 product's rounding), which keeps about 16 significant bits per stage.
+//
+// Thread m of the CTA owns GEMM row m and tensor-memory lane m.  Stage A rows are
+// m = 8 n1 + r (vector r); stage B rows m = 8 k2 + r, so after stage B thread m holds
+// X[k2 + 16 k1] for all k1 -- which, with 16 = 16, is exactly the stage-A row that the
+// next transform (inverse after forward and back) needs: the passes chain the inverse
+// and forward transforms with the pointwise multiply between them in registers.
+//
+// Row pass (IFFT, transmit, FFT): vectors are 8 rows.  Column pass (FFT, propagate,
+// IFFT): vectors are 8 consecutive columns.  Both gather and scatter straight to global
+// memory (a warp's load touches 8 rows x 4 elements, or 4 rows x 8 columns), so a CTA's
+// shared memory is only its operand tiles and tables and several CTAs per SM overlap
+// their MMA latencies.  Both are persistent over tiles, allocate 32 tensor-memory
+// columns per CTA once, and give up a bounded mbarrier wait by setting the device error
+// word.
+#include <cuda_bf16.h>
+
+#include <string>
+
+#include "engine.h"
+#include "umma.cuh"
+#include "wave_tma.cuh"
+
+namespace emsim_gb300 {
+namespace {
+
+constexpr int N = 256, NS = 16, R = 8, THREADS = 128;
+constexpr int KB = 2 * NS;                  // GEMM K and N (re/im of 16 points)
+constexpr int K_BYTES = KB * 2;             // bf16 bytes per operand row
+constexpr int A_BYTES = 128 * K_BYTES;      // 8 KB
+constexpr int M_BYTES = KB * K_BYTES;       // 2 KB
+constexpr uint32_t LBO = 128, SBO = 8 * K_BYTES;
+constexpr uint32_t TMEM_COLS = 32;
+
+struct __align__(1024) DftSmem {
+    unsigned char a_hi[A_BYTES];
+    unsigned char a_lo[A_BYTES];
+    unsigned char fwd_hi[M_BYTES], fwd_lo[M_BYTES], inv_hi[M_BYTES], inv_lo[M_BYTES];
+    float2 tw[N];  // W256^m
+    uint64_t bar;
+    uint32_t tmem;
+    int pad;
+};
+
+__device__ __forceinline__ void split2(float re, float im, __nv_bfloat162& hi, __nv_bfloat162& lo) {
+    hi = __floats2bfloat162_rn(re, im);
+    const float2 h = __bfloat1622float2(hi);
+    lo = __floats2bfloat162_rn(re - h.x, im - h.y);
+}
+
+// DFT matrices and twiddles from the FP64-derived table exp(-2 pi i m / 4096)
+__device__ void init_tables(DftSmem& s, const float2* __restrict__ tw4096) {
+    for (int e = threadIdx.x; e < KB * KB; e += blockDim.x) {
+        const int j = e / KB, i = e % KB;  // output column j = 2 k + c, input i = 2 n + p
+        const int k = j >> 1, c = j & 1, n = i >> 1, p = i & 1;
+        const float2 w = __ldg(tw4096 + ((n * k) & 15) * 256);  // W16^(n k)
+        // out re: re_in * wr - im_in * wi ; out im: re_in * wi + im_in * wr
+        const float vf = c == 0 ? (p == 0 ? w.x : -w.y) : (p == 0 ? w.y : w.x);
+        const float vi = c == 0 ? (p == 0 ? w.x : w.y) : (p == 0 ? -w.y : w.x);  // conj(W)
+        const uint32_t off = umma::kmajor_offset<K_BYTES>(j, i);
+        const __nv_bfloat16 fh = __float2bfloat16_rn(vf), ih = __float2bfloat16_rn(vi);
+        *reinterpret_cast<__nv_bfloat16*>(s.fwd_hi + off) = fh;
+        *reinterpret_cast<__nv_bfloat16*>(s.fwd_lo + off) = __float2bfloat16_rn(vf - __bfloat162float(fh));
+        *reinterpret_cast<__nv_bfloat16*>(s.inv_hi + off) = ih;
+        *reinterpret_cast<__nv_bfloat16*>(s.inv_lo + off) = __float2bfloat16_rn(vi - __bfloat162float(ih));
+    }
+    for (int m = threadIdx.x; m < N; m += blockDim.x) s.tw[m] = __ldg(tw4096 + m * 16);
+}
+
+// thread m writes its own GEMM row: 16 complex values z[n], K positions 2n, 2n + 1
+__device__ __forceinline__ void write_row(DftSmem& s, int m, const float2 (&z)[NS]) {
+#pragma unroll
+    for (int g = 0; g < NS / 4; ++g) {  // 4 complex = 16 bytes = one core-matrix row
+        __nv_bfloat162 h[4], l[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) split2(z[4 * g + q].x, z[4 * g + q].y, h[q], l[q]);
+        const uint32_t off = umma::kmajor_offset<K_BYTES>(m, 8 * g);
+        *reinterpret_cast<uint4*>(s.a_hi + off) = *reinterpret_cast<uint4*>(h);
+        *reinterpret_cast<uint4*>(s.a_lo + off) = *reinterpret_cast<uint4*>(l);
+    }
+}
+
+// stage-A output Y[n1][k2] (thread m = 8 n1 + r) -> twiddle -> stage-B rows 8 k2 + r, K 2 n1
+template <bool INV>
+__device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m, const float (&d)[KB]) {
+    const int n1 = m >> 3, r = m & 7;
+#pragma unroll
+    for (int k2 = 0; k2 < NS; ++k2) {
+        float2 w = s.tw[n1 * k2];
+        if (INV) w.y = -w.y;
+        const float re = d[2 * k2] * w.x - d[2 * k2 + 1] * w.y;
+        const float im = d[2 * k2] * w.y + d[2 * k2 + 1] * w.x;
+        __nv_bfloat162 h, l;
+        split2(re, im, h, l);
+        const uint32_t off = umma::kmajor_offset<K_BYTES>(8 * k2 + r, 2 * n1);
+        *reinterpret_cast<__nv_bfloat162*>(s.a_hi + off) = h;
+        *reinterpret_cast<__nv_bfloat162*>(s.a_lo + off) = l;
+    }
+}
+
+// one 16-point stage on the A tile: 6 MMAs (hi.hi, hi.lo, lo.hi over 2 K steps), then
+// every thread reads its D row; false when the completion wait timed out
+template <bool INV>
+__device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB]) {
+    tma::fence_proxy_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        umma::fence_after_sync();
+        const unsigned char* mh = INV ? s.inv_hi : s.fwd_hi;
+        const unsigned char* ml = INV ? s.inv_lo : s.fwd_lo;
+        constexpr uint32_t idesc = umma::idesc_bf16_f32(128, KB);
+#pragma unroll
+        for (int ks = 0; ks < KB / 16; ++ks) {
+            const uint64_t ah = umma::smem_desc(s.a_hi + ks * 2 * LBO, LBO, SBO);
+            const uint64_t al = umma::smem_desc(s.a_lo + ks * 2 * LBO, LBO, SBO);
+            const uint64_t bh = umma::smem_desc(mh + ks * 2 * LBO, LBO, SBO);
+            const uint64_t bl = umma::smem_desc(ml + ks * 2 * LBO, LBO, SBO);
+            umma::mma_bf16(s.tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
+            umma::mma_bf16(s.tmem, ah, bl, idesc, 1u);
+            umma::mma_bf16(s.tmem, al, bh, idesc, 1u);
+        }
+        umma::commit(&s.bar);
+    }
+    const bool ok = tma::mbar_wait(&s.bar, phase);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) return false;
+    umma::fence_after_sync();
+    const uint32_t base = umma::taddr(s.tmem, (threadIdx.x >> 5) * 32, 0);
+#pragma unroll
+    for (int c = 0; c < KB / 8; ++c) {
+        float v[8];
+        umma::ld_x8(base + 8 * c, v);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) d[8 * c + i] = v[i];
+    }
+    umma::ld_wait();
+    return true;
+}
+
+__device__ void setup(DftSmem& s, const float2* tw4096) {
+    if (threadIdx.x < 32) {
+        umma::tmem_alloc(&s.tmem, TMEM_COLS);
+        umma::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        tma::mbar_init(&s.bar, 1);
+        tma::fence_mbar_init();
+    }
+    init_tables(s, tw4096);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+}
+
+// ok == false: a completion wait gave up; wait once more (bounded) for the MMAs in
+// flight before the tensor memory is freed
+__device__ void teardown(DftSmem& s, bool ok, uint32_t phase) {
+    if (!ok) tma::mbar_wait(&s.bar, phase ^ 1u);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) umma::tmem_dealloc(s.tmem, TMEM_COLS);
+}
+
+// ---- row pass: inverse row FFT, x exp(i sigma V), forward row FFT ----------------------
+__global__ void __launch_bounds__(THREADS) row_bf16_kernel(RowArgs a, int n_tiles) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
+    setup(s, a.tw);
+    const int m = threadIdx.x;
+    const int hi3 = m >> 3, r = m & 7;  // stage-A row 8 n1 + r / stage-B row 8 k2 + r
+    uint32_t phase = 0;
+    bool ok = true;
+    const int tiles_per_img = a.n_rows / R;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const long long img = tile / tiles_per_img;
+        const int row = (tile - (int)img * tiles_per_img) * R + r;
+        const float2* src = a.in + img * a.in_img_stride + (long long)row * N;
+        const float* vsrc = a.slice + img * a.slice_img_stride + (long long)row * N;
+        float d[KB];
+        {
+            float2 z[NS];
+#pragma unroll
+            for (int n2 = 0; n2 < NS; ++n2) z[n2] = src[hi3 + NS * n2];
+            write_row(s, m, z);
+        }
+        if (!(ok = stage<true>(s, phase, d))) break;
+        twiddle_scatter<true>(s, m, d);
+        if (!(ok = stage<true>(s, phase, d))) break;
+        {
+            // thread m = 8 k2 + r holds psi[k2 + 16 k1]: transmit, then it is the forward
+            // transform's stage-A row 8 n1 + r with n1 = k2, n2 = k1
+            float2 z[NS];
+#pragma unroll
+            for (int k1 = 0; k1 < NS; ++k1) {
+                float sn, cs;
+                sincosf(a.sigma * __ldg(vsrc + hi3 + NS * k1), &sn, &cs);
+                z[k1] = cmul(make_float2(d[2 * k1], d[2 * k1 + 1]), make_float2(cs, sn));
+            }
+            write_row(s, m, z);
+        }
+        if (!(ok = stage<false>(s, phase, d))) break;
+        twiddle_scatter<false>(s, m, d);
+        if (!(ok = stage<false>(s, phase, d))) break;
+        float2* dst = a.out + img * a.out_img_stride + (long long)row * N;
+#pragma unroll
+        for (int k1 = 0; k1 < NS; ++k1) dst[hi3 + NS * k1] = make_float2(d[2 * k1], d[2 * k1 + 1]);
+    }
+    if (!ok && m == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
+    teardown(s, ok, phase);
+}
+
+// ---- column pass: forward column FFT, x P(k) inside the band-limit / N, inverse --------
+__global__ void __launch_bounds__(THREADS) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
+                                                          int n_img) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
+    setup(s, a.tw);
+    const int m = threadIdx.x;
+    const int hi3 = m >> 3, c = m & 7;  // stage-A row 8 n1 + c / stage-B row 8 k2 + c
+    uint32_t phase = 0;
+    bool ok = true;
+    const int live_per_img = lt_lo + lt_hi;
+    const int n_tiles = live_per_img * n_img;
+    const long long ld = a.n_cols;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int img = tile / live_per_img;
+        const int j = tile - img * live_per_img;
+        const int col = (j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo)) * R + c;
+        float2* base = a.data + (long long)img * a.img_stride + col;
+        float d[KB];
+        {
+            float2 z[NS];
+#pragma unroll
+            for (int n2 = 0; n2 < NS; ++n2) z[n2] = base[(hi3 + NS * n2) * ld];
+            write_row(s, m, z);
+        }
+        if (!(ok = stage<false>(s, phase, d))) break;
+        twiddle_scatter<false>(s, m, d);
+        if (!(ok = stage<false>(s, phase, d))) break;
+        {
+            // thread m = 8 k2 + c holds X[k] at k = k2 + 16 k1 of its column
+            const int k2a = abs(fftfreq_int(col, a.n_cols));
+            const float2 p2 = __ldg(a.p2 + col);
+            float2 z[NS];
+#pragma unroll
+            for (int k1 = 0; k1 < NS; ++k1) {
+                const float4 q = __ldg(a.p1 + hi3 + NS * k1);
+                const float2 v = make_float2(d[2 * k1], d[2 * k1 + 1]);
+                z[k1] = (k2a <= __float_as_int(q.z)) ? cmul(v, cmul(make_float2(q.x, q.y), p2)) : make_float2(0.f, 0.f);
+            }
+            write_row(s, m, z);
+        }
+        if (!(ok = stage<true>(s, phase, d))) break;
+        twiddle_scatter<true>(s, m, d);
+        if (!(ok = stage<true>(s, phase, d))) break;
+#pragma unroll
+        for (int k1 = 0; k1 < NS; ++k1) base[(hi3 + NS * k1) * ld] = make_float2(d[2 * k1], d[2 * k1 + 1]);
+    }
+    if (ok) {  // dead tiles: outside the band-limit in every row
+        const int dead_per_img = tiles_per_img - live_per_img;
+        for (int t = blockIdx.x; t < dead_per_img * n_img; t += gridDim.x) {
+            const int img = t / dead_per_img;
+            float2* base = a.data + (long long)img * a.img_stride + (lt_lo + t - img * dead_per_img) * R + c;
+#pragma unroll
+            for (int q = 0; q < N / 16; ++q) base[(hi3 + 16 * q) * ld] = make_float2(0.f, 0.f);
+        }
+    } else if (m == 0) {
+        atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
+    }
+    teardown(s, ok, phase);
+}
+
+constexpr size_t ROW_SMEM = sizeof(DftSmem);
+constexpr size_t COL_SMEM = sizeof(DftSmem);
+
+}  // namespace
+
+// 0: plain FP32 passes; 1: split-BF16 tensor-core passes where they exist (length 256)
+static int g_precision = 0;
+
+int precision_mode() { return g_precision; }
+
+bool launch_row_bf16(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st, int* status) {
+    if (g_precision != 1 || n2 != N || ops != (ROW_IFFT | ROW_TRANSMIT | ROW_FFT) || a.n_rows % R != 0) return false;
+    const int n_tiles = (a.n_rows / R) * n_img;
+    *status = ensure_smem_attr((const void*)row_bf16_kernel, ROW_SMEM);
+    if (*status != EMSIM_GB300_OK) return true;
+    const int grid = persistent_grid((const void*)row_bf16_kernel, THREADS, ROW_SMEM, n_tiles);
+    row_bf16_kernel<<<grid, THREADS, ROW_SMEM, st>>>(a, n_tiles);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(std::string("split-bf16 row pass launch: ") + cudaGetErrorString(e));
+        *status = EMSIM_GB300_ERR_CUDA;
+    } else {
+        *status = EMSIM_GB300_OK;
+    }
+    return true;
+}
+
+bool launch_col_bf16(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st, int* status) {
+    if (g_precision != 1 || n1 != N || mode != COL_PROPAGATE || a.n_cols % R != 0) return false;
+    const int tiles_per_img = a.n_cols / R;
+    const LiveTiles lt = live_tiles(a, R, tiles_per_img);
+    *status = ensure_smem_attr((const void*)col_bf16_kernel, COL_SMEM);
+    if (*status != EMSIM_GB300_OK) return true;
+    const int grid = persistent_grid((const void*)col_bf16_kernel, THREADS, COL_SMEM, tiles_per_img * n_img);
+    col_bf16_kernel<<<grid, THREADS, COL_SMEM, st>>>(a, tiles_per_img, lt.lo, lt.hi, n_img);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(std::string("split-bf16 column pass launch: ") + cudaGetErrorString(e));
+        *status = EMSIM_GB300_ERR_CUDA;
+    } else {
+        *status = EMSIM_GB300_OK;
+    }
+    return true;
+}
+
+}  // namespace emsim_gb300
+
+extern "C" int emsim_gb300_set_precision(int mode) {
+    using namespace emsim_gb300;
+    EMSIM_REQUIRE(mode == 0 || mode == 1, EMSIM_GB300_ERR_INVALID,
+                  "set_precision: 0 (plain FP32) or 1 (split-BF16 tensor-core passes)");
+    g_precision = mode;
+    return EMSIM_GB300_OK;
+}
+
+extern "C" int emsim_gb300_get_precision(void) { return emsim_gb300::precision_mode(); }

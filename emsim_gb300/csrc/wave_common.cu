@@ -183,6 +183,8 @@ PassTuning pass_tuning(int n) {
 }
 
 int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
+    int bf16_status;
+    if (launch_row_bf16(n2, ops, a, n_img, st, &bf16_status)) return bf16_status;
     // the adjoint's extra operands (ROW_STORE_PHI, ROW_GRAD) run on the one-tile-per-CTA kernel
     const bool tma = tma_enabled() && n2 >= 16 && pass_tuning(n2).row_tma != 0 && !(ops & (ROW_STORE_PHI | ROW_GRAD)) &&
                      ((ops & ROW_CONST_IN) || aligned16(a.in)) &&
@@ -206,6 +208,8 @@ int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
 }
 
 int launch_col(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st) {
+    int bf16_status;
+    if (launch_col_bf16(n1, mode, a, n_img, st, &bf16_status)) return bf16_status;
     const bool tma = tma_enabled() && n1 >= 16 && pass_tuning(n1).col_tma != 0 && col_tma_B(n1, a.n_cols) >= 2 &&
                      aligned16(a.data);
     if (tma) {

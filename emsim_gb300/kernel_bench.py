@@ -54,6 +54,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--autotune", action="store_true", help="tune the pass kernels for --n first")
     ap.add_argument("--tuning-from-cache", action="store_true", help="apply the cached tuning for --n")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16x3"])
     args = ap.parse_args(argv)
     dev = torch.device("cuda", torch.cuda.current_device())
     torch.manual_seed(0)
@@ -61,7 +62,8 @@ def main(argv=None):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     st = lambda: ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)  # noqa: E731
     P = backend._ptr
-    out = {"case": args.case, "n": n}
+    out = {"case": args.case, "n": n, "precision": args.precision}
+    backend.set_precision(args.precision)
     if args.autotune or args.tuning_from_cache:
         from . import autotune
         out["tuning"] = autotune.ensure(n, n) if args.tuning_from_cache else autotune.tune(n, n, batch=B)

@@ -306,6 +306,18 @@ int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int col_tma, i
 int emsim_gb300_get_pass_tuning(int n, int* out);
 
 /* ---------------------------------------------------------------------------------
+ * Precision mode of the wave passes (no counterpart in the reference, which computes in
+ * FP32 through cuFFT / FFTW).  0: plain FP32 Stockham passes (default).  1: split-BF16
+ * tensor-core passes where they exist: 256-point rows and columns of the multislice step
+ * (row inverse FFT + transmit + forward FFT, column FFT + propagate + inverse FFT) run as
+ * two 16-point DFT GEMMs per transform on tcgen05 with bf16 hi + lo operands and fp32
+ * accumulation (about 16 significant bits per stage); every other pass stays FP32.
+ * Process-wide.
+ * ------------------------------------------------------------------------------- */
+int emsim_gb300_set_precision(int mode);
+int emsim_gb300_get_precision(void);
+
+/* ---------------------------------------------------------------------------------
  * Ragged batches: molecules of one lateral size with different slice counts in one call.
  * No counterpart in the reference, which builds and propagates one molecule at a time
  * (pipe.py:46-55, simulator.py:71-91).
