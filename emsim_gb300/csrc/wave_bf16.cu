@@ -18,6 +18,11 @@
 // next transform (inverse after forward and back) needs: the passes chain the inverse
 // and forward transforms with the pointwise multiply between them in registers.
 //
+// The inverse transform reuses the forward matrix: IDFT(x) = conj(DFT(conj(x))), and
+// through the four steps the conjugations meet at the twiddle, so the inverse is "write
+// conj(x), forward stage, forward twiddle, forward stage, read conj(D)" -- sign flips in
+// registers only.
+//
 // Row pass (IFFT, transmit, FFT): vectors are 8 rows.  Column pass (FFT, propagate,
 // IFFT): vectors are 8 consecutive columns.  Both gather and scatter straight to global
 // memory (a warp's load touches 8 rows x 4 elements, or 4 rows x 8 columns), so a CTA's
@@ -27,6 +32,9 @@
 // word.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "engine.h"
@@ -44,11 +52,12 @@ constexpr int M_BYTES = KB * K_BYTES;       // 2 KB
 constexpr uint32_t LBO = 128, SBO = 8 * K_BYTES;
 constexpr uint32_t TMEM_COLS = 32;
 
-struct __align__(1024) DftSmem {
+struct __align__(128) DftSmem {
     unsigned char a_hi[A_BYTES];
     unsigned char a_lo[A_BYTES];
-    unsigned char fwd_hi[M_BYTES], fwd_lo[M_BYTES], inv_hi[M_BYTES], inv_lo[M_BYTES];
+    unsigned char fwd_hi[M_BYTES], fwd_lo[M_BYTES];
     float2 tw[N];  // W256^m
+    float4 p1[N];  // column pass: the propagator's row factors (ColArgs::p1)
     uint64_t bar;
     uint32_t tmem;
     int pad;
@@ -68,24 +77,26 @@ __device__ void init_tables(DftSmem& s, const float2* __restrict__ tw4096) {
         const float2 w = __ldg(tw4096 + ((n * k) & 15) * 256);  // W16^(n k)
         // out re: re_in * wr - im_in * wi ; out im: re_in * wi + im_in * wr
         const float vf = c == 0 ? (p == 0 ? w.x : -w.y) : (p == 0 ? w.y : w.x);
-        const float vi = c == 0 ? (p == 0 ? w.x : w.y) : (p == 0 ? -w.y : w.x);  // conj(W)
         const uint32_t off = umma::kmajor_offset<K_BYTES>(j, i);
-        const __nv_bfloat16 fh = __float2bfloat16_rn(vf), ih = __float2bfloat16_rn(vi);
+        const __nv_bfloat16 fh = __float2bfloat16_rn(vf);
         *reinterpret_cast<__nv_bfloat16*>(s.fwd_hi + off) = fh;
         *reinterpret_cast<__nv_bfloat16*>(s.fwd_lo + off) = __float2bfloat16_rn(vf - __bfloat162float(fh));
-        *reinterpret_cast<__nv_bfloat16*>(s.inv_hi + off) = ih;
-        *reinterpret_cast<__nv_bfloat16*>(s.inv_lo + off) = __float2bfloat16_rn(vi - __bfloat162float(ih));
     }
     for (int m = threadIdx.x; m < N; m += blockDim.x) s.tw[m] = __ldg(tw4096 + m * 16);
 }
 
-// thread m writes its own GEMM row: 16 complex values z[n], K positions 2n, 2n + 1
-__device__ __forceinline__ void write_row(DftSmem& s, int m, const float2 (&z)[NS]) {
+// thread m writes its own GEMM row: 16 complex values (v[2n], v[2n + 1]), conjugated when
+// CONJ, at K positions 2n, 2n + 1
+template <bool CONJ>
+__device__ __forceinline__ void write_row(DftSmem& s, int m, const float (&v)[KB]) {
 #pragma unroll
     for (int g = 0; g < NS / 4; ++g) {  // 4 complex = 16 bytes = one core-matrix row
         __nv_bfloat162 h[4], l[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) split2(z[4 * g + q].x, z[4 * g + q].y, h[q], l[q]);
+        for (int q = 0; q < 4; ++q) {
+            const int n = 4 * g + q;
+            split2(v[2 * n], CONJ ? -v[2 * n + 1] : v[2 * n + 1], h[q], l[q]);
+        }
         const uint32_t off = umma::kmajor_offset<K_BYTES>(m, 8 * g);
         *reinterpret_cast<uint4*>(s.a_hi + off) = *reinterpret_cast<uint4*>(h);
         *reinterpret_cast<uint4*>(s.a_lo + off) = *reinterpret_cast<uint4*>(l);
@@ -93,13 +104,11 @@ __device__ __forceinline__ void write_row(DftSmem& s, int m, const float2 (&z)[N
 }
 
 // stage-A output Y[n1][k2] (thread m = 8 n1 + r) -> twiddle -> stage-B rows 8 k2 + r, K 2 n1
-template <bool INV>
 __device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m, const float (&d)[KB]) {
     const int n1 = m >> 3, r = m & 7;
 #pragma unroll
     for (int k2 = 0; k2 < NS; ++k2) {
-        float2 w = s.tw[n1 * k2];
-        if (INV) w.y = -w.y;
+        const float2 w = s.tw[n1 * k2];
         const float re = d[2 * k2] * w.x - d[2 * k2 + 1] * w.y;
         const float im = d[2 * k2] * w.y + d[2 * k2 + 1] * w.x;
         __nv_bfloat162 h, l;
@@ -112,15 +121,14 @@ __device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m, const float (
 
 // one 16-point stage on the A tile: 6 MMAs (hi.hi, hi.lo, lo.hi over 2 K steps), then
 // every thread reads its D row; false when the completion wait timed out
-template <bool INV>
 __device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB]) {
     tma::fence_proxy_async();
     umma::fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0) {
         umma::fence_after_sync();
-        const unsigned char* mh = INV ? s.inv_hi : s.fwd_hi;
-        const unsigned char* ml = INV ? s.inv_lo : s.fwd_lo;
+        const unsigned char* mh = s.fwd_hi;
+        const unsigned char* ml = s.fwd_lo;
         constexpr uint32_t idesc = umma::idesc_bf16_f32(128, KB);
 #pragma unroll
         for (int ks = 0; ks < KB / 16; ++ks) {
@@ -150,7 +158,7 @@ __device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB
     return true;
 }
 
-__device__ void setup(DftSmem& s, const float2* tw4096) {
+__device__ void setup(DftSmem& s, const float2* tw4096, const float4* p1 = nullptr) {
     if (threadIdx.x < 32) {
         umma::tmem_alloc(&s.tmem, TMEM_COLS);
         umma::tmem_relinquish();
@@ -160,6 +168,8 @@ __device__ void setup(DftSmem& s, const float2* tw4096) {
         tma::fence_mbar_init();
     }
     init_tables(s, tw4096);
+    if (p1)
+        for (int m = threadIdx.x; m < N; m += blockDim.x) s.p1[m] = __ldg(p1 + m);
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
@@ -190,30 +200,30 @@ __global__ void __launch_bounds__(THREADS) row_bf16_kernel(RowArgs a, int n_tile
         const float2* src = a.in + img * a.in_img_stride + (long long)row * N;
         const float* vsrc = a.slice + img * a.slice_img_stride + (long long)row * N;
         float d[KB];
-        {
-            float2 z[NS];
 #pragma unroll
-            for (int n2 = 0; n2 < NS; ++n2) z[n2] = src[hi3 + NS * n2];
-            write_row(s, m, z);
+        for (int n2 = 0; n2 < NS; ++n2) {
+            const float2 v = src[hi3 + NS * n2];
+            d[2 * n2] = v.x;
+            d[2 * n2 + 1] = v.y;
         }
-        if (!(ok = stage<true>(s, phase, d))) break;
-        twiddle_scatter<true>(s, m, d);
-        if (!(ok = stage<true>(s, phase, d))) break;
-        {
-            // thread m = 8 k2 + r holds psi[k2 + 16 k1]: transmit, then it is the forward
-            // transform's stage-A row 8 n1 + r with n1 = k2, n2 = k1
-            float2 z[NS];
+        write_row<true>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        // thread m = 8 k2 + r holds conj(psi[k2 + 16 k1]): transmit, then it is the forward
+        // transform's stage-A row 8 n1 + r with n1 = k2, n2 = k1
 #pragma unroll
-            for (int k1 = 0; k1 < NS; ++k1) {
-                float sn, cs;
-                sincosf(a.sigma * __ldg(vsrc + hi3 + NS * k1), &sn, &cs);
-                z[k1] = cmul(make_float2(d[2 * k1], d[2 * k1 + 1]), make_float2(cs, sn));
-            }
-            write_row(s, m, z);
+        for (int k1 = 0; k1 < NS; ++k1) {
+            float sn, cs;
+            sincosf(a.sigma * __ldg(vsrc + hi3 + NS * k1), &sn, &cs);
+            const float2 t = cmul(make_float2(d[2 * k1], -d[2 * k1 + 1]), make_float2(cs, sn));
+            d[2 * k1] = t.x;
+            d[2 * k1 + 1] = t.y;
         }
-        if (!(ok = stage<false>(s, phase, d))) break;
-        twiddle_scatter<false>(s, m, d);
-        if (!(ok = stage<false>(s, phase, d))) break;
+        write_row<false>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
         float2* dst = a.out + img * a.out_img_stride + (long long)row * N;
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) dst[hi3 + NS * k1] = make_float2(d[2 * k1], d[2 * k1 + 1]);
@@ -223,51 +233,54 @@ __global__ void __launch_bounds__(THREADS) row_bf16_kernel(RowArgs a, int n_tile
 }
 
 // ---- column pass: forward column FFT, x P(k) inside the band-limit / N, inverse --------
-__global__ void __launch_bounds__(THREADS) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
+__global__ void __launch_bounds__(THREADS, 8) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
                                                           int n_img) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
-    setup(s, a.tw);
+    setup(s, a.tw, a.p1);
     const int m = threadIdx.x;
     const int hi3 = m >> 3, c = m & 7;  // stage-A row 8 n1 + c / stage-B row 8 k2 + c
     uint32_t phase = 0;
     bool ok = true;
     const int live_per_img = lt_lo + lt_hi;
     const int n_tiles = live_per_img * n_img;
-    const long long ld = a.n_cols;
+    const int ld = a.n_cols;  // (row, col) offsets below 2^31: 256 rows x n_cols
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const int img = tile / live_per_img;
         const int j = tile - img * live_per_img;
         const int col = (j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo)) * R + c;
         float2* base = a.data + (long long)img * a.img_stride + col;
         float d[KB];
-        {
-            float2 z[NS];
 #pragma unroll
-            for (int n2 = 0; n2 < NS; ++n2) z[n2] = base[(hi3 + NS * n2) * ld];
-            write_row(s, m, z);
+        for (int n2 = 0; n2 < NS; ++n2) {
+            const float2 v = base[(hi3 + NS * n2) * ld];
+            d[2 * n2] = v.x;
+            d[2 * n2 + 1] = v.y;
         }
-        if (!(ok = stage<false>(s, phase, d))) break;
-        twiddle_scatter<false>(s, m, d);
-        if (!(ok = stage<false>(s, phase, d))) break;
+        write_row<false>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
         {
             // thread m = 8 k2 + c holds X[k] at k = k2 + 16 k1 of its column
             const int k2a = abs(fftfreq_int(col, a.n_cols));
             const float2 p2 = __ldg(a.p2 + col);
-            float2 z[NS];
 #pragma unroll
             for (int k1 = 0; k1 < NS; ++k1) {
-                const float4 q = __ldg(a.p1 + hi3 + NS * k1);
+                const float4 q = s.p1[hi3 + NS * k1];
                 const float2 v = make_float2(d[2 * k1], d[2 * k1 + 1]);
-                z[k1] = (k2a <= __float_as_int(q.z)) ? cmul(v, cmul(make_float2(q.x, q.y), p2)) : make_float2(0.f, 0.f);
+                const float2 t = (k2a <= __float_as_int(q.z)) ? cmul(v, cmul(make_float2(q.x, q.y), p2))
+                                                              : make_float2(0.f, 0.f);
+                d[2 * k1] = t.x;
+                d[2 * k1 + 1] = t.y;
             }
-            write_row(s, m, z);
         }
-        if (!(ok = stage<true>(s, phase, d))) break;
-        twiddle_scatter<true>(s, m, d);
-        if (!(ok = stage<true>(s, phase, d))) break;
+        write_row<true>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
 #pragma unroll
-        for (int k1 = 0; k1 < NS; ++k1) base[(hi3 + NS * k1) * ld] = make_float2(d[2 * k1], d[2 * k1 + 1]);
+        for (int k1 = 0; k1 < NS; ++k1) base[(hi3 + NS * k1) * ld] = make_float2(d[2 * k1], -d[2 * k1 + 1]);
     }
     if (ok) {  // dead tiles: outside the band-limit in every row
         const int dead_per_img = tiles_per_img - live_per_img;
@@ -286,6 +299,46 @@ __global__ void __launch_bounds__(THREADS) col_bf16_kernel(ColArgs a, int tiles_
 constexpr size_t ROW_SMEM = sizeof(DftSmem);
 constexpr size_t COL_SMEM = sizeof(DftSmem);
 
+// Persistent grid of a tensor-memory kernel.  The occupancy API reports one resident CTA
+// per SM for any kernel that allocates tensor memory, so residency is computed here from
+// the kernel's registers and shared memory, the SM's limits and the 512 tensor-memory
+// columns (TMEM_COLS per CTA).  A CTA beyond what fits waits for a slot, which costs
+// time but not correctness: CTAs never wait on one another.
+int tmem_grid(const void* func, size_t smem, int n_tiles) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find({dev, func});
+        if (it != cache.end()) {
+            per_sm = it->second;
+        } else {
+            cudaFuncAttributes fa{};
+            int smem_sm = 0, regs_sm = 0, reserved = 0, thr_sm = 0, blk_sm = 0;
+            cudaFuncGetAttributes(&fa, func);
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+            cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+            cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+            cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+            cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev);
+            const int regs_cta = ((fa.numRegs + 7) / 8) * 8 * THREADS;
+            per_sm = std::min(512 / (int)TMEM_COLS, thr_sm / THREADS);
+            per_sm = std::min(per_sm, blk_sm);
+            if (regs_cta > 0) per_sm = std::min(per_sm, regs_sm / regs_cta);
+            per_sm = std::min(per_sm, (int)(smem_sm / (smem + fa.sharedSizeBytes + reserved)));
+            if (per_sm < 1) per_sm = 1;
+            cache[{dev, func}] = per_sm;
+        }
+    }
+    int n_sm = 0;
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    const long long g = std::min<long long>((long long)per_sm * std::max(n_sm, 1), n_tiles);
+    return g < 1 ? 1 : (int)g;
+}
+
 }  // namespace
 
 // 0: plain FP32 passes; 1: split-BF16 tensor-core passes where they exist (length 256)
@@ -298,7 +351,7 @@ bool launch_row_bf16(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t 
     const int n_tiles = (a.n_rows / R) * n_img;
     *status = ensure_smem_attr((const void*)row_bf16_kernel, ROW_SMEM);
     if (*status != EMSIM_GB300_OK) return true;
-    const int grid = persistent_grid((const void*)row_bf16_kernel, THREADS, ROW_SMEM, n_tiles);
+    const int grid = tmem_grid((const void*)row_bf16_kernel, ROW_SMEM, n_tiles);
     row_bf16_kernel<<<grid, THREADS, ROW_SMEM, st>>>(a, n_tiles);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -316,7 +369,7 @@ bool launch_col_bf16(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t
     const LiveTiles lt = live_tiles(a, R, tiles_per_img);
     *status = ensure_smem_attr((const void*)col_bf16_kernel, COL_SMEM);
     if (*status != EMSIM_GB300_OK) return true;
-    const int grid = persistent_grid((const void*)col_bf16_kernel, THREADS, COL_SMEM, tiles_per_img * n_img);
+    const int grid = tmem_grid((const void*)col_bf16_kernel, COL_SMEM, tiles_per_img * n_img);
     col_bf16_kernel<<<grid, THREADS, COL_SMEM, st>>>(a, tiles_per_img, lt.lo, lt.hi, n_img);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
