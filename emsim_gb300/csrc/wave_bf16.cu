@@ -13,10 +13,12 @@
 // the bf16 product's rounding), which keeps about 16 significant bits per stage.
 //
 // Thread m of the CTA owns GEMM row m and tensor-memory lane m.  Stage A rows are
-// m = 8 n1 + r (vector r); stage B rows m = 8 k2 + r, so after stage B thread m holds
+// m = row(r, n1) (vector r); stage B rows m = row(r, k2), so after stage B thread m holds
 // X[k2 + 16 k1] for all k1 -- which, with 16 = 16, is exactly the stage-A row that the
 // next transform (inverse after forward and back) needs: the passes chain the inverse
-// and forward transforms with the pointwise multiply between them in registers.
+// and forward transforms with the pointwise multiply between them in registers.  The row
+// pass uses row(r, i) = 16 r + i (a warp reads and writes 128 contiguous bytes of two
+// rows), the column pass row(c, i) = 8 i + c (a warp covers eight adjacent columns).
 //
 // The inverse transform reuses the forward matrix: IDFT(x) = conj(DFT(conj(x))), and
 // through the four steps the conjugations meet at the twiddle, so the inverse is "write
@@ -47,9 +49,18 @@ namespace {
 constexpr int N = 256, NS = 16, R = 8, THREADS = 128;
 constexpr int KB = 2 * NS;                  // GEMM K and N (re/im of 16 points)
 constexpr int K_BYTES = KB * 2;             // bf16 bytes per operand row
-constexpr int A_BYTES = 128 * K_BYTES;      // 8 KB
-constexpr int M_BYTES = KB * K_BYTES;       // 2 KB
-constexpr uint32_t LBO = 128, SBO = 8 * K_BYTES;
+// K-major operand tiles without swizzle, padded so that neither the row writes nor the
+// twiddle scatter meet bank conflicts: the four 8 x 16-byte core matrices of a row group
+// sit LBO = 144 bytes apart (4 banks of skew), row groups SBO = 608 bytes apart (16
+// banks of skew between groups two apart)
+constexpr uint32_t LBO = 144, SBO = 608;
+constexpr int A_BYTES = (128 / 8) * SBO;
+constexpr int M_BYTES = (KB / 8) * SBO;
+static_assert(3 * LBO + 128 <= SBO, "row groups overlap");
+
+__host__ __device__ constexpr uint32_t kmajor(int r, int k) {
+    return (uint32_t)((r >> 3) * SBO + (k >> 3) * LBO + (r & 7) * 16 + (k & 7) * 2);
+}
 constexpr uint32_t TMEM_COLS = 32;
 
 struct __align__(128) DftSmem {
@@ -77,7 +88,7 @@ __device__ void init_tables(DftSmem& s, const float2* __restrict__ tw4096) {
         const float2 w = __ldg(tw4096 + ((n * k) & 15) * 256);  // W16^(n k)
         // out re: re_in * wr - im_in * wi ; out im: re_in * wi + im_in * wr
         const float vf = c == 0 ? (p == 0 ? w.x : -w.y) : (p == 0 ? w.y : w.x);
-        const uint32_t off = umma::kmajor_offset<K_BYTES>(j, i);
+        const uint32_t off = kmajor(j, i);
         const __nv_bfloat16 fh = __float2bfloat16_rn(vf);
         *reinterpret_cast<__nv_bfloat16*>(s.fwd_hi + off) = fh;
         *reinterpret_cast<__nv_bfloat16*>(s.fwd_lo + off) = __float2bfloat16_rn(vf - __bfloat162float(fh));
@@ -97,15 +108,34 @@ __device__ __forceinline__ void write_row(DftSmem& s, int m, const float (&v)[KB
             const int n = 4 * g + q;
             split2(v[2 * n], CONJ ? -v[2 * n + 1] : v[2 * n + 1], h[q], l[q]);
         }
-        const uint32_t off = umma::kmajor_offset<K_BYTES>(m, 8 * g);
+        const uint32_t off = kmajor(m, 8 * g);
         *reinterpret_cast<uint4*>(s.a_hi + off) = *reinterpret_cast<uint4*>(h);
         *reinterpret_cast<uint4*>(s.a_lo + off) = *reinterpret_cast<uint4*>(l);
     }
 }
 
-// stage-A output Y[n1][k2] (thread m = 8 n1 + r) -> twiddle -> stage-B rows 8 k2 + r, K 2 n1
+// GEMM row of (vector v, index i) in a tile of R = 8 vectors: VEC_MAJOR puts a vector's
+// 16 indices in consecutive rows (m = 16 v + i: a warp covers two vectors, so its global
+// accesses along a row are 128-byte contiguous), else m = 8 i + v (a warp covers eight
+// vectors: eight consecutive columns)
+template <bool VEC_MAJOR>
+__device__ __forceinline__ int gemm_row(int v, int i) {
+    return VEC_MAJOR ? 16 * v + i : 8 * i + v;
+}
+template <bool VEC_MAJOR>
+__device__ __forceinline__ int row_vec(int m) {
+    return VEC_MAJOR ? m >> 4 : m & 7;
+}
+template <bool VEC_MAJOR>
+__device__ __forceinline__ int row_idx(int m) {
+    return VEC_MAJOR ? m & 15 : m >> 3;
+}
+
+// stage-A output Y[n1][k2] of vector r (thread m = gemm_row(r, n1)) -> twiddle ->
+// stage-B rows gemm_row(r, k2), K 2 n1
+template <bool VEC_MAJOR>
 __device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m, const float (&d)[KB]) {
-    const int n1 = m >> 3, r = m & 7;
+    const int n1 = row_idx<VEC_MAJOR>(m), r = row_vec<VEC_MAJOR>(m);
 #pragma unroll
     for (int k2 = 0; k2 < NS; ++k2) {
         const float2 w = s.tw[n1 * k2];
@@ -113,7 +143,7 @@ __device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m, const float (
         const float im = d[2 * k2] * w.y + d[2 * k2 + 1] * w.x;
         __nv_bfloat162 h, l;
         split2(re, im, h, l);
-        const uint32_t off = umma::kmajor_offset<K_BYTES>(8 * k2 + r, 2 * n1);
+        const uint32_t off = kmajor(gemm_row<VEC_MAJOR>(r, k2), 2 * n1);
         *reinterpret_cast<__nv_bfloat162*>(s.a_hi + off) = h;
         *reinterpret_cast<__nv_bfloat162*>(s.a_lo + off) = l;
     }
@@ -142,7 +172,8 @@ __device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB
         }
         umma::commit(&s.bar);
     }
-    const bool ok = tma::mbar_wait(&s.bar, phase);
+    // one warp polls the completion; the others wait at the barrier without issuing
+    const bool ok = threadIdx.x >= 32 || tma::mbar_wait(&s.bar, phase);
     phase ^= 1u;
     if (__syncthreads_or(!ok)) return false;
     umma::fence_after_sync();
@@ -185,12 +216,13 @@ __device__ void teardown(DftSmem& s, bool ok, uint32_t phase) {
 }
 
 // ---- row pass: inverse row FFT, x exp(i sigma V), forward row FFT ----------------------
-__global__ void __launch_bounds__(THREADS) row_bf16_kernel(RowArgs a, int n_tiles) {
+__global__ void __launch_bounds__(THREADS, 7) row_bf16_kernel(RowArgs a, int n_tiles) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
     setup(s, a.tw);
     const int m = threadIdx.x;
-    const int hi3 = m >> 3, r = m & 7;  // stage-A row 8 n1 + r / stage-B row 8 k2 + r
+    // row r of the tile; stage-A index n1 = lo4, stage-B index k2 = lo4
+    const int r = row_vec<true>(m), lo4 = row_idx<true>(m);
     uint32_t phase = 0;
     bool ok = true;
     const int tiles_per_img = a.n_rows / R;
@@ -199,47 +231,50 @@ __global__ void __launch_bounds__(THREADS) row_bf16_kernel(RowArgs a, int n_tile
         const int row = (tile - (int)img * tiles_per_img) * R + r;
         const float2* src = a.in + img * a.in_img_stride + (long long)row * N;
         const float* vsrc = a.slice + img * a.slice_img_stride + (long long)row * N;
-        float d[KB];
+        float d[KB], pot[NS];
 #pragma unroll
         for (int n2 = 0; n2 < NS; ++n2) {
-            const float2 v = src[hi3 + NS * n2];
+            const float2 v = src[lo4 + NS * n2];
             d[2 * n2] = v.x;
             d[2 * n2 + 1] = v.y;
         }
+#pragma unroll
+        for (int k1 = 0; k1 < NS; ++k1) pot[k1] = __ldg(vsrc + lo4 + NS * k1);  // used after the inverse
         write_row<true>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
-        twiddle_scatter(s, m, d);
+        twiddle_scatter<true>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
-        // thread m = 8 k2 + r holds conj(psi[k2 + 16 k1]): transmit, then it is the forward
-        // transform's stage-A row 8 n1 + r with n1 = k2, n2 = k1
+        // thread (r, k2) holds conj(psi[k2 + 16 k1]): transmit, then it is the forward
+        // transform's stage-A row (r, n1) with n1 = k2, n2 = k1
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) {
             float sn, cs;
-            sincosf(a.sigma * __ldg(vsrc + hi3 + NS * k1), &sn, &cs);
+            sincosf(a.sigma * pot[k1], &sn, &cs);
             const float2 t = cmul(make_float2(d[2 * k1], -d[2 * k1 + 1]), make_float2(cs, sn));
             d[2 * k1] = t.x;
             d[2 * k1 + 1] = t.y;
         }
         write_row<false>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
-        twiddle_scatter(s, m, d);
+        twiddle_scatter<true>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
         float2* dst = a.out + img * a.out_img_stride + (long long)row * N;
 #pragma unroll
-        for (int k1 = 0; k1 < NS; ++k1) dst[hi3 + NS * k1] = make_float2(d[2 * k1], d[2 * k1 + 1]);
+        for (int k1 = 0; k1 < NS; ++k1) dst[lo4 + NS * k1] = make_float2(d[2 * k1], d[2 * k1 + 1]);
     }
     if (!ok && m == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
     teardown(s, ok, phase);
 }
 
 // ---- column pass: forward column FFT, x P(k) inside the band-limit / N, inverse --------
-__global__ void __launch_bounds__(THREADS, 8) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
+__global__ void __launch_bounds__(THREADS, 7) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
                                                           int n_img) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
     setup(s, a.tw, a.p1);
     const int m = threadIdx.x;
-    const int hi3 = m >> 3, c = m & 7;  // stage-A row 8 n1 + c / stage-B row 8 k2 + c
+    // column c of the tile; stage-A index n1 = hi3, stage-B index k2 = hi3
+    const int c = row_vec<false>(m), hi3 = row_idx<false>(m);
     uint32_t phase = 0;
     bool ok = true;
     const int live_per_img = lt_lo + lt_hi;
@@ -259,10 +294,10 @@ __global__ void __launch_bounds__(THREADS, 8) col_bf16_kernel(ColArgs a, int til
         }
         write_row<false>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
-        twiddle_scatter(s, m, d);
+        twiddle_scatter<false>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
         {
-            // thread m = 8 k2 + c holds X[k] at k = k2 + 16 k1 of its column
+            // thread (c, k2) holds X[k] at k = k2 + 16 k1 of its column
             const int k2a = abs(fftfreq_int(col, a.n_cols));
             const float2 p2 = __ldg(a.p2 + col);
 #pragma unroll
@@ -277,7 +312,7 @@ __global__ void __launch_bounds__(THREADS, 8) col_bf16_kernel(ColArgs a, int til
         }
         write_row<true>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
-        twiddle_scatter(s, m, d);
+        twiddle_scatter<false>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) base[(hi3 + NS * k1) * ld] = make_float2(d[2 * k1], -d[2 * k1 + 1]);
