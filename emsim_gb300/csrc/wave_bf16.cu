@@ -216,7 +216,7 @@ __device__ void teardown(DftSmem& s, bool ok, uint32_t phase) {
 }
 
 // ---- row pass: inverse row FFT, x exp(i sigma V), forward row FFT ----------------------
-__global__ void __launch_bounds__(THREADS, 7) row_bf16_kernel(RowArgs a, int n_tiles) {
+__global__ void __launch_bounds__(THREADS, 5) row_bf16_kernel(RowArgs a, int n_tiles) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
     setup(s, a.tw);
@@ -226,21 +226,38 @@ __global__ void __launch_bounds__(THREADS, 7) row_bf16_kernel(RowArgs a, int n_t
     uint32_t phase = 0;
     bool ok = true;
     const int tiles_per_img = a.n_rows / R;
-    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        const long long img = tile / tiles_per_img;
-        const int row = (tile - (int)img * tiles_per_img) * R + r;
+    // row r of `tile` as (image, row)
+    auto row_of = [&](int tile, long long& img, int& row) {
+        img = tile / tiles_per_img;
+        row = (tile - (int)img * tiles_per_img) * R + r;
+    };
+    // the next tile's wave is loaded while the current one is transformed
+    float nx[KB];
+    auto load = [&](int tile) {
+        long long img;
+        int row;
+        row_of(tile, img, row);
         const float2* src = a.in + img * a.in_img_stride + (long long)row * N;
-        const float* vsrc = a.slice + img * a.slice_img_stride + (long long)row * N;
-        float d[KB], pot[NS];
 #pragma unroll
         for (int n2 = 0; n2 < NS; ++n2) {
             const float2 v = src[lo4 + NS * n2];
-            d[2 * n2] = v.x;
-            d[2 * n2 + 1] = v.y;
+            nx[2 * n2] = v.x;
+            nx[2 * n2 + 1] = v.y;
         }
+    };
+    if (blockIdx.x < n_tiles) load(blockIdx.x);
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        long long img;
+        int row;
+        row_of(tile, img, row);
+        const float* vsrc = a.slice + img * a.slice_img_stride + (long long)row * N;
+        float d[KB], pot[NS];
+#pragma unroll
+        for (int i = 0; i < KB; ++i) d[i] = nx[i];
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) pot[k1] = __ldg(vsrc + lo4 + NS * k1);  // used after the inverse
         write_row<true>(s, m, d);
+        if (tile + (int)gridDim.x < n_tiles) load(tile + gridDim.x);
         if (!(ok = stage(s, phase, d))) break;
         twiddle_scatter<true>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
@@ -267,7 +284,7 @@ __global__ void __launch_bounds__(THREADS, 7) row_bf16_kernel(RowArgs a, int n_t
 }
 
 // ---- column pass: forward column FFT, x P(k) inside the band-limit / N, inverse --------
-__global__ void __launch_bounds__(THREADS, 7) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
+__global__ void __launch_bounds__(THREADS, 5) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
                                                           int n_img) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
@@ -280,19 +297,35 @@ __global__ void __launch_bounds__(THREADS, 7) col_bf16_kernel(ColArgs a, int til
     const int live_per_img = lt_lo + lt_hi;
     const int n_tiles = live_per_img * n_img;
     const int ld = a.n_cols;  // (row, col) offsets below 2^31: 256 rows x n_cols
-    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        const int img = tile / live_per_img;
+    // column c of live tile `tile` as (image, column)
+    auto col_of = [&](int tile, int& img, int& col) {
+        img = tile / live_per_img;
         const int j = tile - img * live_per_img;
-        const int col = (j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo)) * R + c;
-        float2* base = a.data + (long long)img * a.img_stride + col;
-        float d[KB];
+        col = (j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo)) * R + c;
+    };
+    // the next tile's columns are loaded while the current one is transformed
+    float nx[KB];
+    auto load = [&](int tile) {
+        int img, col;
+        col_of(tile, img, col);
+        const float2* base = a.data + (long long)img * a.img_stride + col;
 #pragma unroll
         for (int n2 = 0; n2 < NS; ++n2) {
             const float2 v = base[(hi3 + NS * n2) * ld];
-            d[2 * n2] = v.x;
-            d[2 * n2 + 1] = v.y;
+            nx[2 * n2] = v.x;
+            nx[2 * n2 + 1] = v.y;
         }
+    };
+    if (blockIdx.x < n_tiles) load(blockIdx.x);
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        int img, col;
+        col_of(tile, img, col);
+        float2* base = a.data + (long long)img * a.img_stride + col;
+        float d[KB];
+#pragma unroll
+        for (int i = 0; i < KB; ++i) d[i] = nx[i];
         write_row<false>(s, m, d);
+        if (tile + (int)gridDim.x < n_tiles) load(tile + gridDim.x);
         if (!(ok = stage(s, phase, d))) break;
         twiddle_scatter<false>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
