@@ -52,6 +52,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// try_wait that may suspend the thread for up to `hint_ns` (it resumes when the phase
+// completes), so a waiting warp takes no issue slots from the warps that have work
+__device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase with the given parity, suspending between polls; false after
+// WAIT_LIMIT_NS without completion.
+__device__ __forceinline__ bool mbar_wait_suspend(uint64_t* bar, uint32_t parity) {
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait_suspend(bar, parity, 100000u)) return true;
+        if (global_ns() - t0 > WAIT_LIMIT_NS) return false;
+    }
+}
+
 // Wait for the phase with the given parity; false after WAIT_LIMIT_NS without completion.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (mbar_try_wait(bar, parity)) return true;

@@ -62,6 +62,7 @@ __host__ __device__ constexpr uint32_t kmajor(int r, int k) {
     return (uint32_t)((r >> 3) * SBO + (k >> 3) * LBO + (r & 7) * 16 + (k & 7) * 2);
 }
 constexpr uint32_t TMEM_COLS = 32;
+constexpr int WAIT_WARPS = 1;
 
 struct __align__(128) DftSmem {
     unsigned char a_hi[A_BYTES];
@@ -172,8 +173,9 @@ __device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB
         }
         umma::commit(&s.bar);
     }
-    // one warp polls the completion; the others wait at the barrier without issuing
-    const bool ok = threadIdx.x >= 32 || tma::mbar_wait(&s.bar, phase);
+    // the first WAIT_WARPS warps wait for the completion (suspended, not spinning); the
+    // others wait at the barrier
+    const bool ok = threadIdx.x >= 32 * WAIT_WARPS || tma::mbar_wait_suspend(&s.bar, phase);
     phase ^= 1u;
     if (__syncthreads_or(!ok)) return false;
     umma::fence_after_sync();
@@ -216,7 +218,7 @@ __device__ void teardown(DftSmem& s, bool ok, uint32_t phase) {
 }
 
 // ---- row pass: inverse row FFT, x exp(i sigma V), forward row FFT ----------------------
-__global__ void __launch_bounds__(THREADS, 5) row_bf16_kernel(RowArgs a, int n_tiles) {
+__global__ void __launch_bounds__(THREADS, 6) row_bf16_kernel(RowArgs a, int n_tiles) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
     setup(s, a.tw);
@@ -226,38 +228,21 @@ __global__ void __launch_bounds__(THREADS, 5) row_bf16_kernel(RowArgs a, int n_t
     uint32_t phase = 0;
     bool ok = true;
     const int tiles_per_img = a.n_rows / R;
-    // row r of `tile` as (image, row)
-    auto row_of = [&](int tile, long long& img, int& row) {
-        img = tile / tiles_per_img;
-        row = (tile - (int)img * tiles_per_img) * R + r;
-    };
-    // the next tile's wave is loaded while the current one is transformed
-    float nx[KB];
-    auto load = [&](int tile) {
-        long long img;
-        int row;
-        row_of(tile, img, row);
-        const float2* src = a.in + img * a.in_img_stride + (long long)row * N;
-#pragma unroll
-        for (int n2 = 0; n2 < NS; ++n2) {
-            const float2 v = src[lo4 + NS * n2];
-            nx[2 * n2] = v.x;
-            nx[2 * n2 + 1] = v.y;
-        }
-    };
-    if (blockIdx.x < n_tiles) load(blockIdx.x);
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        long long img;
-        int row;
-        row_of(tile, img, row);
+        const long long img = tile / tiles_per_img;
+        const int row = (tile - (int)img * tiles_per_img) * R + r;
+        const float2* src = a.in + img * a.in_img_stride + (long long)row * N;
         const float* vsrc = a.slice + img * a.slice_img_stride + (long long)row * N;
         float d[KB], pot[NS];
 #pragma unroll
-        for (int i = 0; i < KB; ++i) d[i] = nx[i];
+        for (int n2 = 0; n2 < NS; ++n2) {
+            const float2 v = src[lo4 + NS * n2];
+            d[2 * n2] = v.x;
+            d[2 * n2 + 1] = v.y;
+        }
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) pot[k1] = __ldg(vsrc + lo4 + NS * k1);  // used after the inverse
         write_row<true>(s, m, d);
-        if (tile + (int)gridDim.x < n_tiles) load(tile + gridDim.x);
         if (!(ok = stage(s, phase, d))) break;
         twiddle_scatter<true>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
@@ -284,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, 5) row_bf16_kernel(RowArgs a, int n_t
 }
 
 // ---- column pass: forward column FFT, x P(k) inside the band-limit / N, inverse --------
-__global__ void __launch_bounds__(THREADS, 5) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
+__global__ void __launch_bounds__(THREADS, 6) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
                                                           int n_img) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
@@ -297,35 +282,19 @@ __global__ void __launch_bounds__(THREADS, 5) col_bf16_kernel(ColArgs a, int til
     const int live_per_img = lt_lo + lt_hi;
     const int n_tiles = live_per_img * n_img;
     const int ld = a.n_cols;  // (row, col) offsets below 2^31: 256 rows x n_cols
-    // column c of live tile `tile` as (image, column)
-    auto col_of = [&](int tile, int& img, int& col) {
-        img = tile / live_per_img;
-        const int j = tile - img * live_per_img;
-        col = (j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo)) * R + c;
-    };
-    // the next tile's columns are loaded while the current one is transformed
-    float nx[KB];
-    auto load = [&](int tile) {
-        int img, col;
-        col_of(tile, img, col);
-        const float2* base = a.data + (long long)img * a.img_stride + col;
-#pragma unroll
-        for (int n2 = 0; n2 < NS; ++n2) {
-            const float2 v = base[(hi3 + NS * n2) * ld];
-            nx[2 * n2] = v.x;
-            nx[2 * n2 + 1] = v.y;
-        }
-    };
-    if (blockIdx.x < n_tiles) load(blockIdx.x);
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        int img, col;
-        col_of(tile, img, col);
+        const int img = tile / live_per_img;
+        const int j = tile - img * live_per_img;
+        const int col = (j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo)) * R + c;
         float2* base = a.data + (long long)img * a.img_stride + col;
         float d[KB];
 #pragma unroll
-        for (int i = 0; i < KB; ++i) d[i] = nx[i];
+        for (int n2 = 0; n2 < NS; ++n2) {
+            const float2 v = base[(hi3 + NS * n2) * ld];
+            d[2 * n2] = v.x;
+            d[2 * n2 + 1] = v.y;
+        }
         write_row<false>(s, m, d);
-        if (tile + (int)gridDim.x < n_tiles) load(tile + gridDim.x);
         if (!(ok = stage(s, phase, d))) break;
         twiddle_scatter<false>(s, m, d);
         if (!(ok = stage(s, phase, d))) break;
