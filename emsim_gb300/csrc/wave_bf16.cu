@@ -69,17 +69,11 @@ struct __align__(128) DftSmem {
     unsigned char a_lo[A_BYTES];
     unsigned char fwd_hi[M_BYTES], fwd_lo[M_BYTES];
     float2 tw[NS * NS];  // tw[16 k2 + n1] = W256^(n1 k2): a warp's 16 n1 read 16 adjacent entries
+    float4 p1[N];  // column pass: the propagator's row factors (ColArgs::p1)
     uint64_t bar;
     uint32_t tmem;
     int pad;
 };
-// the column pass keeps the propagator's row factors (ColArgs::p1) after DftSmem
-constexpr size_t ROW_SMEM = sizeof(DftSmem);
-constexpr size_t COL_SMEM = sizeof(DftSmem) + N * sizeof(float4);
-
-__device__ __forceinline__ const float4* col_p1(const DftSmem& s) {
-    return reinterpret_cast<const float4*>(reinterpret_cast<const unsigned char*>(&s) + sizeof(DftSmem));
-}
 
 __device__ __forceinline__ void split2(float re, float im, __nv_bfloat162& hi, __nv_bfloat162& lo) {
     hi = __floats2bfloat162_rn(re, im);
@@ -87,7 +81,7 @@ __device__ __forceinline__ void split2(float re, float im, __nv_bfloat162& hi, _
     lo = __floats2bfloat162_rn(re - h.x, im - h.y);
 }
 
-// DFT matrix and twiddles from the FP64-derived table exp(-2 pi i m / 4096)
+// DFT matrices and twiddles from the FP64-derived table exp(-2 pi i m / 4096)
 __device__ void init_tables(DftSmem& s, const float2* __restrict__ tw4096) {
     for (int e = threadIdx.x; e < KB * KB; e += blockDim.x) {
         const int j = e / KB, i = e % KB;  // output column j = 2 k + c, input i = 2 n + p
@@ -106,16 +100,22 @@ __device__ void init_tables(DftSmem& s, const float2* __restrict__ tw4096) {
     }
 }
 
-// four complex values (v[0..7] as re, im pairs), conjugated when CONJ, into K positions
-// 8 g .. 8 g + 7 of GEMM row m: one 16-byte store per operand half
+// thread m writes its own GEMM row: 16 complex values (v[2n], v[2n + 1]), conjugated when
+// CONJ, at K positions 2n, 2n + 1
 template <bool CONJ>
-__device__ __forceinline__ void write_group(DftSmem& s, int m, int g, const float* v) {
-    __nv_bfloat162 h[4], l[4];
+__device__ __forceinline__ void write_row(DftSmem& s, int m, const float (&v)[KB]) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) split2(v[2 * q], CONJ ? -v[2 * q + 1] : v[2 * q + 1], h[q], l[q]);
-    const uint32_t off = kmajor(m, 8 * g);
-    *reinterpret_cast<uint4*>(s.a_hi + off) = *reinterpret_cast<uint4*>(h);
-    *reinterpret_cast<uint4*>(s.a_lo + off) = *reinterpret_cast<uint4*>(l);
+    for (int g = 0; g < NS / 4; ++g) {  // 4 complex = 16 bytes = one core-matrix row
+        __nv_bfloat162 h[4], l[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int n = 4 * g + q;
+            split2(v[2 * n], CONJ ? -v[2 * n + 1] : v[2 * n + 1], h[q], l[q]);
+        }
+        const uint32_t off = kmajor(m, 8 * g);
+        *reinterpret_cast<uint4*>(s.a_hi + off) = *reinterpret_cast<uint4*>(h);
+        *reinterpret_cast<uint4*>(s.a_lo + off) = *reinterpret_cast<uint4*>(l);
+    }
 }
 
 // GEMM row of (vector v, index i) in a tile of R = 8 vectors: VEC_MAJOR puts a vector's
@@ -135,59 +135,41 @@ __device__ __forceinline__ int row_idx(int m) {
     return VEC_MAJOR ? m & 15 : m >> 3;
 }
 
-// this thread's D row, columns 16 h .. 16 h + 15: complex outputs k = 8 h .. 8 h + 7
-__device__ __forceinline__ void tmem_half(const DftSmem& s, int h, float (&v)[16]) {
-    const uint32_t base = umma::taddr(s.tmem, (threadIdx.x >> 5) * 32, 16 * h);
-    float a[8], b[8];
-    umma::ld_x8(base, a);
-    umma::ld_x8(base + 8, b);
-    umma::ld_wait();
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        v[i] = a[i];
-        v[8 + i] = b[i];
-    }
-}
-
-// stage-A output Y[n1][k2] of vector r (thread m = gemm_row(r, n1), read from tensor
-// memory eight k2 at a time) -> twiddle -> stage-B rows gemm_row(r, k2), K 2 n1
+// stage-A output Y[n1][k2] of vector r (thread m = gemm_row(r, n1)) -> twiddle ->
+// stage-B rows gemm_row(r, k2), K 2 n1
 template <bool VEC_MAJOR>
-__device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m) {
+__device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m, const float (&d)[KB]) {
     const int n1 = row_idx<VEC_MAJOR>(m), r = row_vec<VEC_MAJOR>(m);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float v[16];
-        tmem_half(s, h, v);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int k2 = 8 * h + q;
-            const float2 w = s.tw[NS * k2 + n1];
-            const float re = v[2 * q] * w.x - v[2 * q + 1] * w.y;
-            const float im = v[2 * q] * w.y + v[2 * q + 1] * w.x;
-            __nv_bfloat162 hi, lo;
-            split2(re, im, hi, lo);
-            const uint32_t off = kmajor(gemm_row<VEC_MAJOR>(r, k2), 2 * n1);
-            *reinterpret_cast<__nv_bfloat162*>(s.a_hi + off) = hi;
-            *reinterpret_cast<__nv_bfloat162*>(s.a_lo + off) = lo;
-        }
+    for (int k2 = 0; k2 < NS; ++k2) {
+        const float2 w = s.tw[NS * k2 + n1];
+        const float re = d[2 * k2] * w.x - d[2 * k2 + 1] * w.y;
+        const float im = d[2 * k2] * w.y + d[2 * k2 + 1] * w.x;
+        __nv_bfloat162 h, l;
+        split2(re, im, h, l);
+        const uint32_t off = kmajor(gemm_row<VEC_MAJOR>(r, k2), 2 * n1);
+        *reinterpret_cast<__nv_bfloat162*>(s.a_hi + off) = h;
+        *reinterpret_cast<__nv_bfloat162*>(s.a_lo + off) = l;
     }
 }
 
-// one 16-point stage on the A tile: 6 MMAs (hi.hi, hi.lo, lo.hi over 2 K steps) into
-// tensor memory, then wait for them; false when the completion wait timed out
-__device__ __forceinline__ bool mma_stage(DftSmem& s, uint32_t& phase) {
+// one 16-point stage on the A tile: 6 MMAs (hi.hi, hi.lo, lo.hi over 2 K steps), then
+// every thread reads its D row; false when the completion wait timed out
+__device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB]) {
     tma::fence_proxy_async();
     umma::fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0) {
         umma::fence_after_sync();
+        const unsigned char* mh = s.fwd_hi;
+        const unsigned char* ml = s.fwd_lo;
         constexpr uint32_t idesc = umma::idesc_bf16_f32(128, KB);
 #pragma unroll
         for (int ks = 0; ks < KB / 16; ++ks) {
             const uint64_t ah = umma::smem_desc(s.a_hi + ks * 2 * LBO, LBO, SBO);
             const uint64_t al = umma::smem_desc(s.a_lo + ks * 2 * LBO, LBO, SBO);
-            const uint64_t bh = umma::smem_desc(s.fwd_hi + ks * 2 * LBO, LBO, SBO);
-            const uint64_t bl = umma::smem_desc(s.fwd_lo + ks * 2 * LBO, LBO, SBO);
+            const uint64_t bh = umma::smem_desc(mh + ks * 2 * LBO, LBO, SBO);
+            const uint64_t bl = umma::smem_desc(ml + ks * 2 * LBO, LBO, SBO);
             umma::mma_bf16(s.tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
             umma::mma_bf16(s.tmem, ah, bl, idesc, 1u);
             umma::mma_bf16(s.tmem, al, bh, idesc, 1u);
@@ -200,6 +182,15 @@ __device__ __forceinline__ bool mma_stage(DftSmem& s, uint32_t& phase) {
     phase ^= 1u;
     if (__syncthreads_or(!ok)) return false;
     umma::fence_after_sync();
+    const uint32_t base = umma::taddr(s.tmem, (threadIdx.x >> 5) * 32, 0);
+#pragma unroll
+    for (int c = 0; c < KB / 8; ++c) {
+        float v[8];
+        umma::ld_x8(base + 8 * c, v);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) d[8 * c + i] = v[i];
+    }
+    umma::ld_wait();
     return true;
 }
 
@@ -213,10 +204,8 @@ __device__ void setup(DftSmem& s, const float2* tw4096, const float4* p1 = nullp
         tma::fence_mbar_init();
     }
     init_tables(s, tw4096);
-    if (p1) {
-        float4* dst = const_cast<float4*>(col_p1(s));
-        for (int m = threadIdx.x; m < N; m += blockDim.x) dst[m] = __ldg(p1 + m);
-    }
+    if (p1)
+        for (int m = threadIdx.x; m < N; m += blockDim.x) s.p1[m] = __ldg(p1 + m);
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
@@ -232,7 +221,7 @@ __device__ void teardown(DftSmem& s, bool ok, uint32_t phase) {
 }
 
 // ---- row pass: inverse row FFT, x exp(i sigma V), forward row FFT ----------------------
-__global__ void __launch_bounds__(THREADS, 8) row_bf16_kernel(RowArgs a, int n_tiles) {
+__global__ void __launch_bounds__(THREADS, 6) row_bf16_kernel(RowArgs a, int n_tiles) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
     setup(s, a.tw);
@@ -247,60 +236,47 @@ __global__ void __launch_bounds__(THREADS, 8) row_bf16_kernel(RowArgs a, int n_t
         const int row = (tile - (int)img * tiles_per_img) * R + r;
         const float2* src = a.in + img * a.in_img_stride + (long long)row * N;
         const float* vsrc = a.slice + img * a.slice_img_stride + (long long)row * N;
-        {
-            float d[KB];
+        float d[KB], pot[NS];
 #pragma unroll
-            for (int n2 = 0; n2 < NS; ++n2) {
-                const float2 v = src[lo4 + NS * n2];
-                d[2 * n2] = v.x;
-                d[2 * n2 + 1] = v.y;
-            }
-#pragma unroll
-            for (int g = 0; g < 4; ++g) write_group<true>(s, m, g, d + 8 * g);
+        for (int n2 = 0; n2 < NS; ++n2) {
+            const float2 v = src[lo4 + NS * n2];
+            d[2 * n2] = v.x;
+            d[2 * n2 + 1] = v.y;
         }
-        if (!(ok = mma_stage(s, phase))) break;
-        twiddle_scatter<true>(s, m);
-        if (!(ok = mma_stage(s, phase))) break;
+#pragma unroll
+        for (int k1 = 0; k1 < NS; ++k1) pot[k1] = __ldg(vsrc + lo4 + NS * k1);  // used after the inverse
+        write_row<true>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter<true>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
         // thread (r, k2) holds conj(psi[k2 + 16 k1]): transmit, then it is the forward
         // transform's stage-A row (r, n1) with n1 = k2, n2 = k1
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            float v[16];
-            tmem_half(s, h, v);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                float sn, cs;
-                sincosf(a.sigma * __ldg(vsrc + lo4 + NS * (8 * h + q)), &sn, &cs);
-                const float2 t = cmul(make_float2(v[2 * q], -v[2 * q + 1]), make_float2(cs, sn));
-                v[2 * q] = t.x;
-                v[2 * q + 1] = t.y;
-            }
-            write_group<false>(s, m, 2 * h, v);
-            write_group<false>(s, m, 2 * h + 1, v + 8);
+        for (int k1 = 0; k1 < NS; ++k1) {
+            float sn, cs;
+            sincosf(a.sigma * pot[k1], &sn, &cs);
+            const float2 t = cmul(make_float2(d[2 * k1], -d[2 * k1 + 1]), make_float2(cs, sn));
+            d[2 * k1] = t.x;
+            d[2 * k1 + 1] = t.y;
         }
-        if (!(ok = mma_stage(s, phase))) break;
-        twiddle_scatter<true>(s, m);
-        if (!(ok = mma_stage(s, phase))) break;
+        write_row<false>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter<true>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
         float2* dst = a.out + img * a.out_img_stride + (long long)row * N;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            float v[16];
-            tmem_half(s, h, v);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) dst[lo4 + NS * (8 * h + q)] = make_float2(v[2 * q], v[2 * q + 1]);
-        }
+        for (int k1 = 0; k1 < NS; ++k1) dst[lo4 + NS * k1] = make_float2(d[2 * k1], d[2 * k1 + 1]);
     }
     if (!ok && m == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
     teardown(s, ok, phase);
 }
 
 // ---- column pass: forward column FFT, x P(k) inside the band-limit / N, inverse --------
-__global__ void __launch_bounds__(THREADS, 7) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
+__global__ void __launch_bounds__(THREADS, 6) col_bf16_kernel(ColArgs a, int tiles_per_img, int lt_lo, int lt_hi,
                                                           int n_img) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     DftSmem& s = *reinterpret_cast<DftSmem*>(smem_raw);
     setup(s, a.tw, a.p1);
-    const float4* p1 = col_p1(s);
     const int m = threadIdx.x;
     // column c of the tile; stage-A index n1 = hi3, stage-B index k2 = hi3
     const int c = row_vec<false>(m), hi3 = row_idx<false>(m);
@@ -314,51 +290,37 @@ __global__ void __launch_bounds__(THREADS, 7) col_bf16_kernel(ColArgs a, int til
         const int j = tile - img * live_per_img;
         const int col = (j < lt_lo ? j : tiles_per_img - lt_hi + (j - lt_lo)) * R + c;
         float2* base = a.data + (long long)img * a.img_stride + col;
-        {
-            float d[KB];
+        float d[KB];
 #pragma unroll
-            for (int n2 = 0; n2 < NS; ++n2) {
-                const float2 v = base[(hi3 + NS * n2) * ld];
-                d[2 * n2] = v.x;
-                d[2 * n2 + 1] = v.y;
-            }
-#pragma unroll
-            for (int g = 0; g < 4; ++g) write_group<false>(s, m, g, d + 8 * g);
+        for (int n2 = 0; n2 < NS; ++n2) {
+            const float2 v = base[(hi3 + NS * n2) * ld];
+            d[2 * n2] = v.x;
+            d[2 * n2 + 1] = v.y;
         }
-        if (!(ok = mma_stage(s, phase))) break;
-        twiddle_scatter<false>(s, m);
-        if (!(ok = mma_stage(s, phase))) break;
+        write_row<false>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter<false>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
         {
             // thread (c, k2) holds X[k] at k = k2 + 16 k1 of its column
             const int k2a = abs(fftfreq_int(col, a.n_cols));
             const float2 p2 = __ldg(a.p2 + col);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                float v[16];
-                tmem_half(s, h, v);
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const float4 f = p1[hi3 + NS * (8 * h + q)];
-                    const float2 x = make_float2(v[2 * q], v[2 * q + 1]);
-                    const float2 t = (k2a <= __float_as_int(f.z)) ? cmul(x, cmul(make_float2(f.x, f.y), p2))
-                                                                  : make_float2(0.f, 0.f);
-                    v[2 * q] = t.x;
-                    v[2 * q + 1] = t.y;
-                }
-                write_group<true>(s, m, 2 * h, v);
-                write_group<true>(s, m, 2 * h + 1, v + 8);
+            for (int k1 = 0; k1 < NS; ++k1) {
+                const float4 q = s.p1[hi3 + NS * k1];
+                const float2 v = make_float2(d[2 * k1], d[2 * k1 + 1]);
+                const float2 t = (k2a <= __float_as_int(q.z)) ? cmul(v, cmul(make_float2(q.x, q.y), p2))
+                                                              : make_float2(0.f, 0.f);
+                d[2 * k1] = t.x;
+                d[2 * k1 + 1] = t.y;
             }
         }
-        if (!(ok = mma_stage(s, phase))) break;
-        twiddle_scatter<false>(s, m);
-        if (!(ok = mma_stage(s, phase))) break;
+        write_row<true>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
+        twiddle_scatter<false>(s, m, d);
+        if (!(ok = stage(s, phase, d))) break;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            float v[16];
-            tmem_half(s, h, v);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) base[(hi3 + NS * (8 * h + q)) * ld] = make_float2(v[2 * q], -v[2 * q + 1]);
-        }
+        for (int k1 = 0; k1 < NS; ++k1) base[(hi3 + NS * k1) * ld] = make_float2(d[2 * k1], -d[2 * k1 + 1]);
     }
     if (ok) {  // dead tiles: outside the band-limit in every row
         const int dead_per_img = tiles_per_img - live_per_img;
@@ -373,6 +335,9 @@ __global__ void __launch_bounds__(THREADS, 7) col_bf16_kernel(ColArgs a, int til
     }
     teardown(s, ok, phase);
 }
+
+constexpr size_t ROW_SMEM = sizeof(DftSmem);
+constexpr size_t COL_SMEM = sizeof(DftSmem);
 
 // Persistent grid of a tensor-memory kernel.  The occupancy API reports one resident CTA
 // per SM for any kernel that allocates tensor memory, so residency is computed here from
