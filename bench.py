@@ -223,6 +223,36 @@ def differentiation_extra(torch, reps: int = 3) -> dict:
             "checkpoint_every": autograd.default_every(64)}
 
 
+def precision_extra(torch, db, backend, flush, reps: int = 5):
+    """The bench step (eager launches, L2 flushed) with the multislice passes in FP32 and in
+    split-BF16 on the tensor cores; returns the timing dict and the split-BF16 image of the
+    first blob (its accuracy against FP64 is computed in the CPU leg)."""
+    out, img = {}, None
+    try:
+        for mode in ("fp32", "bf16x3"):
+            backend.set_precision(mode)
+            for _ in range(2):
+                db.run()
+            times = []
+            for _ in range(reps):
+                flush.fill_(1.0)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                db.run()
+                e1.record()
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1) * 1e-3)
+            out[mode] = {"images_per_s": round(db.B * reps / float(sum(times)), 1)}
+            if mode == "bf16x3":
+                img = db.img[0].cpu().numpy()
+    finally:
+        backend.set_precision("fp32")
+    out["workload"] = "the bench step, eager launches (no CUDA graph), L2 flushed before every step"
+    out["bf16x3_passes"] = ("256-point row pass (IFFT, transmit, FFT) and column pass (FFT, propagate, IFFT) as "
+                            "16x16 four-step DFTs on tcgen05, bf16 hi+lo operands, fp32 accumulation")
+    return out, img
+
+
 def batching_extra(torch, p, n_blobs: int = 32, reps: int = 2) -> dict:
     """A mixed batch through Pipe.run_batch: blobs with log-uniform 5k-200k atoms at
     0.1 A^-3, random orientations, roi 256 or 512, every other one in amorphous ice;
@@ -354,6 +384,7 @@ def run_ours(args):
         return
 
     img0 = db.img[0].cpu().numpy()
+    precision, img_bf16 = precision_extra(torch, db, backend, flush)
     diff = differentiation_extra(torch)
     batching = batching_extra(torch, p)
 
@@ -373,7 +404,8 @@ def run_ours(args):
 
     # ---- CPU baseline: the oracle's restatement of the reference numpy path, and the
     # checker's FP64 image of the first benched blob ------------------------------
-    cpu, acc = cpu_baseline(budget_s=args.cpu_seconds, check=(seeds[0], img0))
+    cpu, acc = cpu_baseline(budget_s=args.cpu_seconds, check=(seeds[0], img0, {"bf16x3": img_bf16}))
+    precision["bf16x3"].update(acc.pop("bf16x3", {}))
 
     clocks = clk.summary()
     out = {
@@ -390,6 +422,7 @@ def run_ours(args):
                                            "hbm_frac": round(v["frac"], 4), "images": v["images"]}
                                   for k, v in rl.items()},
         "accuracy": acc,
+        "precision": precision,
         "differentiation": diff,
         "batching": batching,
         "roofline": roofline,
@@ -436,8 +469,9 @@ def _cpu_one(seed: int) -> float:
 
 def cpu_baseline(budget_s: float = 15.0, processes: int = 1, check=None):
     """Images/s of the reference numpy algorithm on host cores (bounded sample).  With
-    ``check`` = (seed, GPU image), also the relative L2 error of that image against the
-    FP64 oracle (outside the timed sample); returns (baseline, accuracy) then."""
+    ``check`` = (seed, GPU image, {name: other GPU image of the same blob}), also the
+    relative L2 errors of those images against the FP64 oracle (outside the timed sample);
+    returns (baseline, accuracy) then."""
     import multiprocessing as mp
     t0 = time.perf_counter()
     n = 0
@@ -465,13 +499,20 @@ def cpu_baseline(budget_s: float = 15.0, processes: int = 1, check=None):
         return base
     from oracle import multislice as om
     W = WORKLOAD
-    seed, img = check
+    seed, img, others = check
     el, xyz = blob(seed)
     ref64 = om.pipe_run(el, xyz, resolution=W["resolution"], slice_thickness=W["slice_thickness"], roi=W["roi"],
                         beam_energy_kev=W["kev"], dose=W["dose"], cs_mm=W["cs_mm"], defocus=W["defocus"],
                         aperture=W["aperture"], semantics="fftw", dtype=np.float64)
-    acc = {"rel_l2_image_vs_fp64": om.rel_l2(img, ref64),
-           "rel_l2_contrast_vs_fp64": om.rel_l2(img - img.mean(), ref64 - ref64.mean())}
+
+    def errs(x):
+        return {"rel_l2_image_vs_fp64": om.rel_l2(x, ref64),
+                "rel_l2_contrast_vs_fp64": om.rel_l2(x - x.mean(), ref64 - ref64.mean())}
+
+    acc = errs(img)
+    for name, other in (others or {}).items():
+        if other is not None:
+            acc[name] = errs(other)
     return base, acc
 
 
