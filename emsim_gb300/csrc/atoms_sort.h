@@ -8,10 +8,6 @@ namespace emsim_gb300 {
 
 constexpr unsigned INVALID_BUCKET = 0xffffffffu;
 
-// bucketed atom item: slice parity in bit 31, row in bits 12..23, column in bits 0..11
-constexpr int ITEM_ROW_SHIFT = 12;
-constexpr unsigned ITEM_FIELD_MASK = 0xfffu;
-
 struct AtomBucketArgs {
     const float* coords = nullptr;       // (n_atoms, 3) float32, columns (z, x, y)
     unsigned n_atoms = 0;
@@ -20,7 +16,7 @@ struct AtomBucketArgs {
     int n_pairs = 0, n1 = 0;
     BinAxis ax0, ax1, ax2;               // slice, row, column axes (CUDA rule)
     unsigned* bucket = nullptr;          // (n_atoms) bucket id or INVALID_BUCKET
-    unsigned* item = nullptr;            // (n_atoms) (slice parity << 31) | (row << 12) | column
+    unsigned* item = nullptr;            // (n_atoms) (slice parity << 31) | column
     unsigned* bucket_count = nullptr;    // (n_buckets) zeroed before the call
 };
 

@@ -15,7 +15,6 @@
 //   C  rows   : W[pair] -> inverse row FFT -> clip(re) -> V[2p], clip(im) -> V[2p+1]
 #pragma once
 
-#include "atoms_sort.h"
 #include "slices.h"
 #include "wave_passes.cuh"
 
@@ -84,23 +83,10 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
 // Pass B straight from bucketed atoms (no histogram).  The row DFT of row r of slice pair
 // (img, e, pair) at column frequency k2 is z = sum over the bucket's atoms of
 // W^(j k2) (even slice) + i W^(j k2) (odd slice), W = exp(-2 pi i / n2): each term is a
-// 2^22-scaled fixed-point table entry and the sum is kept in integers, so it is exact and
-// independent of the order in which the counting sort placed the atoms.  One rounding to
-// float32 follows.  Then, per element: forward column FFT, x T_e; over all elements:
-// inverse column FFT -> W[img, pair].
-//
-// The sums of a plane (img, e, pair) whose buckets all hold at most WQ_SMALL atoms are
-// formed with 32-bit shared-memory atomics into an (n1 rows x B columns) tile: the
-// plane's atoms (contiguous, row in the item) are spread over the CTA, B threads per
-// atom (one per column), so the work is proportional to atoms x columns with no
-// per-row overhead.  A plane with a larger bucket sums row by row in 64 bits.
-template <int N>
-__device__ __forceinline__ int2 wq_entry(const int2* wq, unsigned u, int col, int kmask, int n2) {
-    // the odd slice of the pair reads the i W half of the table
-    const int idx = (((int)(u & ITEM_FIELD_MASK) * col) & kmask) + (int)(u >> 31) * n2;
-    return wq[idx + (idx >> 4)];
-}
-
+// 2^22-scaled fixed-point table entry and the sum is kept in integers (32-bit for buckets
+// of up to 511 atoms, 64-bit beyond), so it is exact and independent of the order in
+// which the counting sort placed the atoms.  One rounding to float32 follows.  Then, per element: forward column FFT, x T_e; over all
+// elements: inverse column FFT -> W[img, pair].
 template <int N>
 __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS) slice_cols_atoms_kernel(SliceArgs a) {
     constexpr int T = N / 8;
@@ -124,58 +110,37 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     __syncthreads();
     constexpr float INV_SCALE = (float)(1.0 / WQ_SCALE);
     const int kmask = a.n2 - 1;
-    // atomics tile (aliases the FFT exchange buffer: N * B * 8 bytes <= (N + N / 8) * B * 8)
-    int* tile_re = reinterpret_cast<int*>(sm);
-    int* tile_im = tile_re + N * B;
     float2 acc[8];
 #pragma unroll
     for (int m = 0; m < 8; ++m) acc[m] = make_float2(0.f, 0.f);
     for (int e = 0; e < a.n_elems; ++e) {
         const unsigned* off = a.bucket_off + ((long long)(img * a.n_elems + e) * a.n_pairs + pair) * N;
         float2 v[8];
-        bool big = false;
-        for (int r = threadIdx.x; r < N; r += blockDim.x) big |= off[r + 1] - off[r] > (unsigned)WQ_SMALL;
-        if (!__syncthreads_or(big)) {
-            for (int i = threadIdx.x; i < 2 * N * B / 4; i += blockDim.x)
-                reinterpret_cast<int4*>(tile_re)[i] = make_int4(0, 0, 0, 0);
-            __syncthreads();
-            const unsigned hi = off[N];
-            for (unsigned k = off[0] + threadIdx.x / B; k < hi; k += blockDim.x / B) {
-                const unsigned u = __ldg(a.items + k);
-                const int row = (int)((u >> ITEM_ROW_SHIFT) & ITEM_FIELD_MASK);
-                const int2 w = wq_entry<N>(wq, u, col, kmask, a.n2);
-                atomicAdd(tile_re + row * B + b, w.x);
-                atomicAdd(tile_im + row * B + b, w.y);
-            }
-            __syncthreads();
 #pragma unroll
-            for (int m = 0; m < 8; ++m) {
-                const int r = t + m * T;
-                v[m] = make_float2((float)tile_re[r * B + b] * INV_SCALE, (float)tile_im[r * B + b] * INV_SCALE);
-            }
-            __syncthreads();  // the FFT below reuses the tile's shared memory
-        } else {
-#pragma unroll
-            for (int m = 0; m < 8; ++m) {
-                const int r = t + m * T;
-                const unsigned lo = off[r], hi = off[r + 1];
-                if (hi - lo <= (unsigned)WQ_SMALL) {
-                    int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
-                    for (unsigned k = lo; k < hi; ++k) {
-                        const int2 w = wq_entry<N>(wq, __ldg(a.items + k), col, kmask, a.n2);
-                        re += w.x;
-                        im += w.y;
-                    }
-                    v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
-                } else {
-                    long long re = 0, im = 0;
-                    for (unsigned k = lo; k < hi; ++k) {
-                        const int2 w = wq_entry<N>(wq, __ldg(a.items + k), col, kmask, a.n2);
-                        re += w.x;
-                        im += w.y;
-                    }
-                    v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
+        for (int m = 0; m < 8; ++m) {
+            const int r = t + m * T;
+            const unsigned lo = off[r], hi = off[r + 1];
+            if (hi - lo <= (unsigned)WQ_SMALL) {
+                int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
+                for (unsigned k = lo; k < hi; ++k) {
+                    const unsigned u = __ldg(a.items + k);
+                    // the odd slice of the pair reads the i W half of the table
+                    const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
+                    const int2 w = wq[idx + (idx >> 4)];
+                    re += w.x;
+                    im += w.y;
                 }
+                v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
+            } else {
+                long long re = 0, im = 0;
+                for (unsigned k = lo; k < hi; ++k) {
+                    const unsigned u = __ldg(a.items + k);
+                    const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
+                    const int2 w = wq[idx + (idx >> 4)];
+                    re += w.x;
+                    im += w.y;
+                }
+                v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
             }
         }
         fft::fft_regs<N, false, false>(v, sm, b, t, addr, a.tw);
