@@ -8,6 +8,7 @@ per group of equal (n_slices, roi).
 """
 from __future__ import annotations
 
+import os
 from collections import defaultdict
 from typing import List, Optional, Sequence, Tuple, Union
 
@@ -103,6 +104,23 @@ class Pipe:
             self._pin_z = torch.empty(cap, dtype=torch.int32, pin_memory=True)
         return self._pin_xyz[:n_atoms], self._pin_z[:n_atoms]
 
+    def _fill_stage(self, mols, offsets, nx, nz):
+        """Copy the molecules' coordinates and Z into the pinned staging buffers; large
+        batches are copied by a small thread pool (numpy releases the GIL in the copy and
+        cast loops), which keeps the host side of ``run_batch`` short next to the GPU's."""
+        def fill(i):
+            nx[offsets[i]:offsets[i + 1]] = mols[i].coordinates
+            nz[offsets[i]:offsets[i + 1]] = mols[i].elements
+
+        if len(mols) < 4 or int(offsets[-1]) < (1 << 18):
+            for i in range(len(mols)):
+                fill(i)
+            return
+        if getattr(self, "_pool", None) is None:
+            from concurrent.futures import ThreadPoolExecutor
+            self._pool = ThreadPoolExecutor(max_workers=max(1, min(8, (os.cpu_count() or 2) // 2)))
+        list(self._pool.map(fill, range(len(mols))))
+
     def run_batch(self, mols: Sequence[atm.AtomList], defocus: Optional[Sequence[float]] = None,
                   to_host: bool = False, rois: Optional[Sequence] = None) -> List:
         """Images of many molecules (optionally one defocus each), in input order.
@@ -131,10 +149,7 @@ class Pipe:
         offsets[1:] = np.cumsum(sizes)
         n_atoms = int(offsets[-1])
         hx, hz = self._stage(n_atoms)
-        nx, nz = hx.numpy(), hz.numpy()
-        for i, mol in enumerate(mols):
-            nx[offsets[i]:offsets[i + 1]] = mol.coordinates
-            nz[offsets[i]:offsets[i + 1]] = mol.elements
+        self._fill_stage(mols, offsets, hx.numpy(), hz.numpy())
         xyz = hx.to(dev, non_blocking=True)
         zz = hz.to(dev, non_blocking=True)
         off = torch.from_numpy(offsets.astype(np.uint32).view(np.int32)).to(dev)
