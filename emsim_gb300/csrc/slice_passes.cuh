@@ -87,6 +87,8 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
 // of up to 511 atoms, 64-bit beyond), so it is exact and independent of the order in
 // which the counting sort placed the atoms.  One rounding to float32 follows.  Then, per element: forward column FFT, x T_e; over all
 // elements: inverse column FFT -> W[img, pair].
+constexpr int ITEM_CACHE = 6144;  // items of one (image, element, pair) plane staged in shared memory
+
 template <int N>
 __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS) slice_cols_atoms_kernel(SliceArgs a) {
     constexpr int T = N / 8;
@@ -107,6 +109,10 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     // which the padding spreads over the banks
     int2* wq = reinterpret_cast<int2*>(sm + (N + N / 8) * B);
     for (int i = threadIdx.x; i < 2 * a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
+    // the plane's bucket offsets and (up to ITEM_CACHE) items, staged in shared memory by
+    // coalesced loads: the sums below then wait on shared, not global, memory per atom
+    unsigned* s_off = reinterpret_cast<unsigned*>(wq + 2 * a.n2 + a.n2 / 8 + 1);
+    unsigned* s_items = s_off + N + 1;
     __syncthreads();
     constexpr float INV_SCALE = (float)(1.0 / WQ_SCALE);
     const int kmask = a.n2 - 1;
@@ -114,16 +120,25 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
 #pragma unroll
     for (int m = 0; m < 8; ++m) acc[m] = make_float2(0.f, 0.f);
     for (int e = 0; e < a.n_elems; ++e) {
-        const unsigned* off = a.bucket_off + ((long long)(img * a.n_elems + e) * a.n_pairs + pair) * N;
+        const unsigned* off_g = a.bucket_off + ((long long)(img * a.n_elems + e) * a.n_pairs + pair) * N;
+        if (e > 0) __syncthreads();  // every thread is done with the previous plane's items
+        for (int i = threadIdx.x; i <= N; i += blockDim.x) s_off[i] = __ldg(off_g + i);
+        __syncthreads();
+        const unsigned base = s_off[0], count = s_off[N] - base;
+        const bool cached = count <= (unsigned)ITEM_CACHE;
+        if (cached)
+            for (unsigned i = threadIdx.x; i < count; i += blockDim.x) s_items[i] = __ldg(a.items + base + i);
+        __syncthreads();
+        const unsigned* items = cached ? s_items : a.items + base;  // indexed from the plane's first item
         float2 v[8];
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
             const int r = t + m * T;
-            const unsigned lo = off[r], hi = off[r + 1];
+            const unsigned lo = s_off[r] - base, hi = s_off[r + 1] - base;
             if (hi - lo <= (unsigned)WQ_SMALL) {
                 int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
                 for (unsigned k = lo; k < hi; ++k) {
-                    const unsigned u = __ldg(a.items + k);
+                    const unsigned u = items[k];
                     // the odd slice of the pair reads the i W half of the table
                     const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
                     const int2 w = wq[idx + (idx >> 4)];
@@ -134,7 +149,7 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
             } else {
                 long long re = 0, im = 0;
                 for (unsigned k = lo; k < hi; ++k) {
-                    const unsigned u = __ldg(a.items + k);
+                    const unsigned u = items[k];
                     const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
                     const int2 w = wq[idx + (idx >> 4)];
                     re += w.x;
@@ -162,7 +177,8 @@ template <int N>
 int slice_cols_atoms_n(const SliceArgs& a, cudaStream_t st) {
     constexpr int T = N / 8;
     const int B = col_B_for(N, a.n2);
-    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(2 * a.n2 + a.n2 / 8 + 1) * sizeof(int2);
+    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(2 * a.n2 + a.n2 / 8 + 1) * sizeof(int2) +
+                        (size_t)(N + 1 + ITEM_CACHE) * sizeof(unsigned);
     EMSIM_TRY(ensure_smem_attr((const void*)slice_cols_atoms_kernel<N>, smem));
     slice_cols_atoms_kernel<N><<<dim3(a.n2 / B, a.n_img * a.n_pairs), B * T, smem, st>>>(a);
     EMSIM_CHECK_LAUNCH();
