@@ -55,9 +55,11 @@ static int make_tw(int n, float2** out) {
 }
 
 // Propagator tables for dz: p1 (n1, 1/N folded in) then p2 (n2).  Tables are computed on
-// the caller's stream the first time a dz is seen and kept; with more than PROP_SLOTS
-// distinct dz values the oldest slot is rewritten (calls with different dz on different
-// streams of one plan must then be ordered by the caller).
+// the caller's stream the first time a dz is seen and kept, with an event recorded after
+// them: a later caller (any stream) waits for that event, so concurrent calls on several
+// streams of one plan read finished tables.  With more than PROP_SLOTS distinct dz values
+// the oldest slot is rewritten (calls with different dz on different streams of one plan
+// must then be ordered by the caller).
 size_t prop_slot_bytes(const emsim_gb300_wave_plan* p) {
     return (size_t)p->n1 * sizeof(float4) + (size_t)p->n2 * sizeof(float2);
 }
@@ -65,8 +67,14 @@ size_t prop_slot_bytes(const emsim_gb300_wave_plan* p) {
 int get_prop(emsim_gb300_wave_plan* p, double dz, cudaStream_t st, const float4** p1, const float2** p2) {
     std::lock_guard<std::mutex> lk(p->mu);
     const size_t sb = prop_slot_bytes(p);
+    // inside a CUDA-graph capture the events are left alone (an event recorded outside
+    // the capture cannot be waited on inside it); the graph orders its own nodes
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    EMSIM_CHECK_CUDA(cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
     for (int i = 0; i < p->prop_used; ++i) {
         if (p->prop_dz[i] == dz) {
+            if (p->prop_ev[i] && !capturing) EMSIM_CHECK_CUDA(cudaStreamWaitEvent(st, p->prop_ev[i], 0));
             *p1 = reinterpret_cast<const float4*>(p->prop + (size_t)i * sb);
             *p2 = reinterpret_cast<const float2*>(*p1 + p->n1);
             return EMSIM_GB300_OK;
@@ -78,6 +86,14 @@ int get_prop(emsim_gb300_wave_plan* p, double dz, cudaStream_t st, const float4*
     const double coef = M_PI * p->wave_length * dz;
     EMSIM_TRY(prop_tables(t1, t2, p->cut, p->n1, p->n2, p->dfx64, p->dfy64, coef,
                           1.0 / ((double)p->n1 * (double)p->n2), st));
+    if (!capturing) {
+        if (!p->prop_ev[slot]) EMSIM_CHECK_CUDA(cudaEventCreateWithFlags(&p->prop_ev[slot], cudaEventDisableTiming));
+        EMSIM_CHECK_CUDA(cudaEventRecord(p->prop_ev[slot], st));
+    } else if (p->prop_ev[slot]) {
+        // the slot's old event no longer describes its tables
+        cudaEventDestroy(p->prop_ev[slot]);
+        p->prop_ev[slot] = nullptr;
+    }
     p->prop_dz[slot] = dz;
     *p1 = t1;
     *p2 = t2;
@@ -240,6 +256,8 @@ int emsim_gb300_wave_plan_create(int n1, int n2, double d1, double d2, double wa
 
 int emsim_gb300_wave_plan_destroy(emsim_gb300_wave_plan* p) {
     if (!p) return EMSIM_GB300_OK;
+    for (cudaEvent_t& e : p->prop_ev)
+        if (e) cudaEventDestroy(e);
     cudaFree(p->tw1);
     cudaFree(p->tw2);
     cudaFree(p->prop);

@@ -30,6 +30,9 @@ struct emsim_gb300_wave_plan {
     int* cut = nullptr;    // band-limit cutoff per row (bandlimit_cutoffs)
     int cut_max = -1;      // largest cutoff over the rows: columns beyond it are dead for propagation
     double prop_dz[emsim_gb300::PROP_SLOTS];
+    // recorded on the stream that computed the slot's tables; callers on other streams
+    // wait for it before reading them
+    cudaEvent_t prop_ev[emsim_gb300::PROP_SLOTS] = {};
     int prop_used = 0;
     int prop_next = 0;
     std::mutex mu;
