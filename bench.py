@@ -149,6 +149,14 @@ class DeviceBatch:
         P = self.backend._ptr
         nat.call("emsim_gb300_build_slices", self.builder._plan.handle, P(self.coords), self.n_atoms,
                  P(self.counts), self.B, P(self.slices), P(self.ws), self.ws_bytes, st)
+        self.run_image()
+
+    def run_image(self):
+        """plane wave -> multislice -> lens -> |psi|^2 of all blobs from the built slices."""
+        import ctypes
+        nat = self.backend._native
+        st = ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+        P = self.backend._ptr
         W = WORKLOAD
         nat.call("emsim_gb300_multislice_image", self.wp._plan.handle, P(self.slices), self.ns,
                  self.ns * self.n * self.n, W["slice_thickness"], W["dose"], W["cs_mm"],
@@ -251,6 +259,78 @@ def precision_extra(torch, db, backend, flush, reps: int = 5):
     out["bf16x3_passes"] = ("256-point row pass (IFFT, transmit, FFT) and column pass (FFT, propagate, IFFT) as "
                             "16x16 four-step DFTs on tcgen05, bf16 hi+lo operands, fp32 accumulation")
     return out, img
+
+
+def plain_cufft_extra(torch, db, backend, flush, reps: int = 3) -> dict:
+    """The reference's CUDA design on the same GPU and the same slices, as a yardstick for
+    the fused passes: per slice a transmit, a cuFFT C2C forward transform, the propagator
+    (band-limit and 1/N folded in) and a cuFFT inverse; then the lens the same way and
+    |psi|^2 (torch.fft = cuFFT plus torch element-wise kernels).  Timed eagerly, L2
+    flushed before every step; the result is checked against the fused image."""
+    from emsim_gb300 import physics
+    W = WORKLOAD
+    n, B, ns, d = db.n, db.B, db.ns, db.pix
+    dev = db.slices.device
+    lam = physics.electron_wave_length_angstrom(W["kev"])
+    gam = physics.electron_relativity_gamma(W["kev"])
+    sigma = float(np.float32(lam) * np.float32(gam))
+    f = torch.fft.fftfreq(n, d=d, dtype=torch.float64, device=dev)
+    f2 = f[:, None] ** 2 + f[None, :] ** 2
+    fmax = 0.5 / d
+    keep = (f2 <= (0.6667 * fmax) ** 2).to(torch.float64)
+    prop = (torch.polar(keep, -math.pi * lam * W["slice_thickness"] * f2) / (n * n)).to(torch.complex64)
+    c1 = 0.5 * math.pi * W["cs_mm"] * 1e7 * lam ** 3
+    c2 = math.pi * W["defocus"] * lam
+    aper = (f2 <= (W["aperture"] / lam) ** 2).to(torch.float64)
+    lens = (torch.polar(aper, -(c1 * f2 * f2 - c2 * f2)) / (n * n)).to(torch.complex64)
+    amp = math.sqrt(W["dose"] * d * d)
+    slices = db.slices
+
+    def image():
+        psi = torch.full((B, n, n), amp, dtype=torch.complex64, device=dev)
+        for s_ in range(ns):
+            psi = psi * torch.polar(torch.ones((), device=dev), sigma * slices[:, s_])
+            psi = torch.fft.ifft2(torch.fft.fft2(psi) * prop, norm="forward")
+        psi = torch.fft.ifft2(torch.fft.fft2(psi) * lens, norm="forward")
+        return psi.real ** 2 + psi.imag ** 2
+
+    for _ in range(2):
+        img = image()
+    times = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        img = image()
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    ours = db.img
+    rel = float(torch.linalg.vector_norm((img - ours).double()) / torch.linalg.vector_norm(ours.double()))
+    # our fused image call on the same slices, timed the same way, in both precisions
+    fused = {}
+    try:
+        for mode in ("fp32", "bf16x3"):
+            backend.set_precision(mode)
+            db.run_image()
+            tf = []
+            for _ in range(reps):
+                flush.fill_(1.0)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                db.run_image()
+                e1.record()
+                e1.synchronize()
+                tf.append(e0.elapsed_time(e1) * 1e-3)
+            fused[mode] = round(B * reps / float(sum(tf)), 1)
+    finally:
+        backend.set_precision("fp32")
+    return {"workload": f"multislice + lens + |psi|^2 of the bench step's {B} stacks of {ns} slices, {n}^2",
+            "design": "per slice: transmit, cuFFT C2C forward, propagate, cuFFT C2C inverse (torch.fft + "
+                      "torch element-wise kernels); eager, L2 flushed",
+            "plain_cufft_images_per_s": round(B * reps / float(sum(times)), 1),
+            "fused_fp32_images_per_s": fused["fp32"], "fused_bf16x3_images_per_s": fused["bf16x3"],
+            "rel_l2_plain_vs_fused": rel}
 
 
 def batching_extra(torch, p, n_blobs: int = 32, reps: int = 2) -> dict:
@@ -384,6 +464,7 @@ def run_ours(args):
         return
 
     img0 = db.img[0].cpu().numpy()
+    plain = plain_cufft_extra(torch, db, backend, flush)
     precision, img_bf16 = precision_extra(torch, db, backend, flush)
     diff = differentiation_extra(torch)
     batching = batching_extra(torch, p)
@@ -423,6 +504,7 @@ def run_ours(args):
                                   for k, v in rl.items()},
         "accuracy": acc,
         "precision": precision,
+        "plain_cufft": plain,
         "differentiation": diff,
         "batching": batching,
         "roofline": roofline,
