@@ -116,3 +116,23 @@ def test_other_sizes_unchanged_in_bf16_mode(eng):
         eng.set_precision("fp32")
     np.testing.assert_array_equal(got, ref)
     assert _native.check_device_error() == 0
+
+
+@pytest.mark.parametrize("n1,n2", [(256, 128), (128, 256), (256, 512)])
+def test_rectangular_waves_mix_bf16_and_fp32_passes(eng, n1, n2):
+    """A side of 256 runs its pass on the tensor cores, the other side stays FP32."""
+    ns, dz, d = 5, 1.5, 0.5
+    rng = np.random.default_rng(n1 + 3 * n2)
+    w = _rand_wave(rng, (2, n1, n2))
+    sl = (np.abs(rng.normal(size=(ns, n1, n2))) * 3).astype(np.float32)
+    wp = eng.WavePropagator(n1, n2, d, d, 200.0)
+    ref32 = np.asarray(wp.multislice_propagate(w, sl, dz).get())
+    eng.set_precision("bf16x3")
+    try:
+        got = np.asarray(wp.multislice_propagate(w, sl, dz).get())
+    finally:
+        eng.set_precision("fp32")
+    o64 = om.WavePropagator(n1, n2, d, d, 200.0, "fftw", np.float64)
+    for b in range(2):
+        assert om.rel_l2(got[b], o64.multislice_propagate(w[b], sl, dz)) < TOL
+    assert 0 < om.rel_l2(got, ref32) < TOL
