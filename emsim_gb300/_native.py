@@ -14,6 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libemsim_gb300.so"
 
 _c_int, _c_ll, _c_dbl, _c_uint, _c_vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_uint, ctypes.c_void_p
 _c_size = ctypes.c_size_t
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
 _pp = ctypes.POINTER(ctypes.c_void_p)
 
 # name -> (restype, argtypes); mirrors include/emsim_gb300.h one to one
@@ -29,6 +30,9 @@ SIGNATURES = {
     "emsim_gb300_singleslice_propagate": (_c_int, [_c_vp, _c_vp, _c_vp, _c_ll, _c_dbl, _c_vp, _c_int, _c_vp]),
     "emsim_gb300_multislice_propagate": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_ll, _c_dbl, _c_vp, _c_int, _c_vp]),
     "emsim_gb300_lens_propagate": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_dbl, _c_dbl, _c_vp, _c_int, _c_vp]),
+    "emsim_gb300_lens_incoherent_workspace_size": (_c_size, [_c_vp, _c_int]),
+    "emsim_gb300_lens_intensity_incoherent": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_dbl_p, _c_dbl_p, _c_int,
+                                                       _c_dbl, _c_dbl, _c_vp, _c_vp, _c_size, _c_vp]),
     "emsim_gb300_intensity": (_c_int, [_c_vp, _c_vp, _c_ll, _c_vp]),
     "emsim_gb300_multislice_image": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_dbl, _c_dbl, _c_dbl,
                                               ctypes.POINTER(ctypes.c_double), _c_int, _c_dbl, _c_vp, _c_vp,

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes
 import logging
+import math
 import threading
 from typing import Dict, List, Optional, Sequence, Tuple
 
@@ -385,6 +386,46 @@ class WavePropagator:
                      float(aperture), _ptr(out), nb, _stream())
         return _wrap(out)
 
+    # -- partial coherence (extension) ---------------------------------------------
+    def lens_intensity_incoherent(self, exit_wave, cs_mm: float, defocus_values, weights, aperture: float,
+                                  illumination_angle: float = 0.0) -> DeviceArray:
+        """sum_k weights[k] * |lens(exit_wave, defocus_values[k])|^2, each lens transfer damped
+        by the quasi-coherent envelope of an illumination semi-angle (rad; 0 = coherent)
+        (``emsim_gb300_lens_intensity_incoherent``).  (n1, n2) or (B, n1, n2) float32."""
+        w, nb = self._wave(exit_wave)
+        d = np.ascontiguousarray(np.atleast_1d(np.asarray(defocus_values, dtype=np.float64)))
+        wt = np.ascontiguousarray(np.atleast_1d(np.asarray(weights, dtype=np.float64)))
+        if d.ndim != 1 or d.shape != wt.shape or d.size < 1:
+            raise ValueError("defocus_values and weights must be equal-length 1-D sequences")
+        n1, n2 = self.wave_shape
+        out = torch.empty((nb, n1, n2), dtype=torch.float32, device=_device())
+        lib = _native.load()
+        nbytes = int(lib.emsim_gb300_lens_incoherent_workspace_size(self._plan.handle, nb))
+        work = torch.empty(nbytes, dtype=torch.uint8, device=_device())
+        dp = ctypes.POINTER(ctypes.c_double)
+        _native.call("emsim_gb300_lens_intensity_incoherent", self._plan.handle, _ptr(w), nb, float(cs_mm),
+                     d.ctypes.data_as(dp), wt.ctypes.data_as(dp), int(d.size), float(illumination_angle),
+                     float(aperture), _ptr(out), _ptr(work), nbytes, _stream())
+        return _wrap(out[0] if w.dim() == 2 else out)
+
+    def image_partially_coherent(self, slices, dz: float, electron_dose: float, cs_mm: float, defocus: float,
+                                 aperture: float, focal_spread: float = 0.0, illumination_angle: float = 0.0,
+                                 n_focal: int = 7, n_batch: Optional[int] = None) -> DeviceArray:
+        """Plane wave -> multislice -> partially coherent lens -> intensity: the focal spread
+        (standard deviation of the defocus, A) as an incoherent sum over n_focal
+        Gauss-Hermite defocus values, the illumination semi-angle (rad) as the
+        quasi-coherent spatial envelope.  ``slices``: (n_slices, n1, n2) shared by n_batch
+        images (default 1) or (B, n_slices, n1, n2)."""
+        s = as_device(slices, torch.float32)
+        nb = int(s.shape[0]) if s.dim() == 4 else (n_batch or 1)
+        n1, n2 = self.wave_shape
+        psi = torch.empty((nb, n1, n2), dtype=torch.complex64, device=_device())
+        _native.call("emsim_gb300_init_wave", self._plan.handle, float(electron_dose), _ptr(psi), nb, _stream())
+        ew = self.multislice_propagate(psi, s, dz)
+        dfs, wts = focal_spread_quadrature(defocus, focal_spread, n_focal)
+        img = self.lens_intensity_incoherent(ew, cs_mm, dfs, wts, aperture, illumination_angle)
+        return _wrap(img.reshape(n1, n2)) if s.dim() == 3 and n_batch is None else img
+
     # -- fused image formation (extension) --------------------------------------
     def image(self, slices, dz: float, electron_dose: float, cs_mm: float, defocus, aperture: float,
               n_batch: Optional[int] = None, return_exit_wave: bool = False):
@@ -413,6 +454,18 @@ class WavePropagator:
         if return_exit_wave:
             return img, _wrap(ew[0] if squeeze else ew)
         return img
+
+
+def focal_spread_quadrature(defocus: float, focal_spread: float, n: int = 7) -> Tuple[np.ndarray, np.ndarray]:
+    """Defocus values and weights of an n-point Gauss-Hermite rule for a Gaussian defocus
+    distribution (mean ``defocus``, standard deviation ``focal_spread``, A); the weights
+    sum to one.  focal_spread = 0 gives the single coherent defocus."""
+    if focal_spread < 0 or n < 1:
+        raise ValueError("focal_spread must be >= 0 and n >= 1")
+    if focal_spread == 0:
+        return np.array([float(defocus)]), np.array([1.0])
+    x, w = np.polynomial.hermite.hermgauss(int(n))
+    return float(defocus) + math.sqrt(2.0) * float(focal_spread) * x, w / math.sqrt(math.pi)
 
 
 def image_ragged(wp: "WavePropagator", stacks, n_slices: Sequence[int], dz: float, electron_dose: float,

@@ -79,6 +79,9 @@ struct ColArgs {
     float lens_scale = 1.f;  // normalisation folded into the transfer function
     int n_c2 = 1;
     double c2v[64] = {};
+    // lens: spatial-coherence envelope exp(-es * f^2 * (2 c1 f^2 - c2)^2), es = (alpha_s /
+    // lambda)^2 for an illumination semi-angle alpha_s (rad); 0: fully coherent
+    double es = 0.0;
 };
 constexpr int LENS_MAX = 64;  // images per lens launch with distinct defocus
 
@@ -132,6 +135,8 @@ int ew_transmit(const float2* in, const float* slice, float2* out, long long n, 
                 long long in_stride, long long slice_stride, long long out_stride, cudaStream_t st);
 int ew_fill(float2* out, long long n, float2 value, cudaStream_t st);
 int ew_intensity(const float2* in, float* out, long long n, cudaStream_t st);
+// y[i] += a * x[i] (float32, one rounding: fmaf)
+int ew_axpy(float* y, const float* x, float a, long long n, cudaStream_t st);
 int ew_propagate(float2* data, const ColArgs& a, int n_img, cudaStream_t st);
 int ew_lens(float2* data, const ColArgs& a, int n_img, cudaStream_t st);
 int prop_tables(float4* p1, float2* p2, const int* cut, int n1, int n2, double dfx64, double dfy64,

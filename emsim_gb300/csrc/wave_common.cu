@@ -356,6 +356,19 @@ int ew_intensity(const float2* in, float* out, long long n, cudaStream_t st) {
     return EMSIM_GB300_OK;
 }
 
+__global__ void axpy_kernel(float* __restrict__ y, const float* __restrict__ x, float a, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = fmaf(a, x[i], y[i]);
+}
+
+int ew_axpy(float* y, const float* x, float a, long long n, cudaStream_t st) {
+    int blocks = ceil_div(n, 256);
+    if (blocks > 8192) blocks = 8192;
+    axpy_kernel<<<blocks, 256, 0, st>>>(y, x, a, n);
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
+}
+
 // full-spectrum multiply by P(k) * band-limit (p1 carries 1/N), for the generic path
 __global__ void propagate_kernel(float2* data, ColArgs a) {
     const long long n = (long long)a.n_rows * a.n_cols;

@@ -107,7 +107,14 @@ __device__ __forceinline__ float2 lens_factor(int k1, int k2, double fy2, double
     chi = fma(-TWO_PI, rint(chi * INV_TWO_PI), chi);  // reduce mod 2 pi in FP64
     float s, c;
     sincosf((float)chi, &s, &c);
-    return make_float2(c * a.lens_scale, -s * a.lens_scale);
+    float scale = a.lens_scale;
+    if (a.es > 0.0) {
+        // quasi-coherent spatial envelope: |grad chi| / (2 pi) = f |Cs lambda^3 f^2 - df lambda|
+        // = f |2 c1 f^2 - c2| / pi, damped by exp(-(pi alpha_s / lambda)^2 |grad chi / 2 pi|^2)
+        const double g = fma(2.0 * a.c1, q, -c2);
+        scale *= (float)exp(-a.es * q * g * g);
+    }
+    return make_float2(c * scale, -s * scale);
 }
 
 // threads per CTA of the column pass: 512 with two CTAs per SM (64 registers), 1024 from

@@ -174,12 +174,13 @@ int g_space(emsim_gb300_wave_plan* p, const float2* in, float2* out, double dz, 
 }
 
 int g_lens(emsim_gb300_wave_plan* p, const float2* in, float2* out, double cs, const double* defocus, int n_def,
-           double aperture, int nb, cudaStream_t st) {
+           double aperture, int nb, cudaStream_t st, double es = 0.0) {
     EMSIM_TRY(g_fft2(p, in, out, false, nb, st));
     for (int i0 = 0; i0 < nb; i0 += LENS_MAX) {
         const int cnt = nb - i0 < LENS_MAX ? nb - i0 : LENS_MAX;
         ColArgs a = base_col(p, out + (size_t)i0 * p->n1 * p->n2);
         set_lens(p, a, cs, aperture, 1.0f / (float)((double)p->n1 * p->n2));
+        a.es = es;
         a.n_c2 = n_def == 1 ? 1 : cnt;
         for (int j = 0; j < a.n_c2; ++j) a.c2v[j] = M_PI * p->wave_length * defocus[(i0 + j) % n_def];
         EMSIM_TRY(ew_lens(a.data, a, cnt, st));
@@ -424,6 +425,58 @@ int emsim_gb300_lens_propagate(emsim_gb300_wave_plan* p, const void* wave, doubl
     EMSIM_TRY(launch_col(p->n1, COL_LENS, c, nb, st));
     r.in = out;
     return launch_row(p->n2, ROW_IFFT, r, nb, st);
+}
+
+size_t emsim_gb300_lens_incoherent_workspace_size(const emsim_gb300_wave_plan* p, int nb) {
+    if (!p || nb < 1) return 0;
+    const size_t npix = (size_t)p->n1 * p->n2 * (size_t)nb;
+    // fast path: row spectrum X and a working copy (complex), one intensity (float)
+    return npix * (2 * sizeof(float2) + sizeof(float)) + 256;
+}
+
+int emsim_gb300_lens_intensity_incoherent(emsim_gb300_wave_plan* p, const void* exit_wave, int nb, double cs_mm,
+                                          const double* defocus, const double* weights, int n_defocus,
+                                          double illumination_angle, double aperture, float* image_out, void* work,
+                                          size_t work_bytes, void* stream) {
+    EMSIM_TRY(check_device(p));
+    EMSIM_REQUIRE(exit_wave && image_out && work && defocus && weights && n_defocus >= 1 && nb >= 1 &&
+                      illumination_angle >= 0.0,
+                  EMSIM_GB300_ERR_INVALID, "lens_intensity_incoherent: bad arguments");
+    EMSIM_REQUIRE(work_bytes >= emsim_gb300_lens_incoherent_workspace_size(p, nb), EMSIM_GB300_ERR_INVALID,
+                  "lens_intensity_incoherent: workspace smaller than lens_incoherent_workspace_size");
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long npix = (long long)p->n1 * p->n2;
+    const long long n_all = npix * nb;
+    float2* x = reinterpret_cast<float2*>(work);
+    float2* y = x + n_all;
+    float* ik = reinterpret_cast<float*>(y + n_all);
+    const double es = (illumination_angle / p->wave_length) * (illumination_angle / p->wave_length);
+    EMSIM_CHECK_CUDA(cudaMemsetAsync(image_out, 0, sizeof(float) * (size_t)n_all, st));
+    RowArgs r = base_row(p);
+    if (p->fast) {
+        r.in = (const float2*)exit_wave;
+        r.out = x;
+        EMSIM_TRY(launch_row(p->n2, ROW_FFT, r, nb, st));
+    }
+    for (int k = 0; k < n_defocus; ++k) {
+        if (p->fast) {
+            EMSIM_CHECK_CUDA(cudaMemcpyAsync(y, x, sizeof(float2) * (size_t)n_all, cudaMemcpyDeviceToDevice, st));
+            ColArgs c = base_col(p, y);
+            set_lens(p, c, cs_mm, aperture, 1.0f / (float)npix);
+            c.es = es;
+            c.n_c2 = 1;
+            c.c2v[0] = M_PI * p->wave_length * defocus[k];
+            EMSIM_TRY(launch_col(p->n1, COL_LENS, c, nb, st));
+            r.in = y;
+            r.out_int = ik;
+            EMSIM_TRY(launch_row(p->n2, ROW_IFFT | ROW_OUT_INTENSITY, r, nb, st));
+        } else {
+            EMSIM_TRY(g_lens(p, (const float2*)exit_wave, y, cs_mm, defocus + k, 1, aperture, nb, st, es));
+            EMSIM_TRY(ew_intensity(y, ik, n_all, st));
+        }
+        EMSIM_TRY(ew_axpy(image_out, ik, (float)weights[k], n_all, st));
+    }
+    return EMSIM_GB300_OK;
 }
 
 int emsim_gb300_intensity(const void* wave, float* out, long long n, void* stream) {

@@ -80,12 +80,20 @@ class Pipe:
 
     def run(self, mol):
         """Image of one molecule, (n1, n2) float32 on the device."""
-        if not self.add_water:
+        if not self.add_water and not self.microscope.partially_coherent:
             return backend._wrap(self.run_batch([mol])[0])
         slices = self.build_slices(mol)
-        m = self.microscope
         wp = self._propagator(slices.shape[-2:])
-        return wp.image(slices, self.slice_thickness, m.electron_dose, m.cs_mm, m.defocus, m.aperture)
+        return self._form_image(wp, slices, self.microscope.defocus)
+
+    def _form_image(self, wp, slices, defocus):
+        """plane wave -> multislice -> lens -> |psi|^2 of one (n_slices, n1, n2) stack,
+        partially coherent when the microscope says so."""
+        m = self.microscope
+        if m.partially_coherent:
+            return wp.image_partially_coherent(slices, self.slice_thickness, m.electron_dose, m.cs_mm, defocus,
+                                               m.aperture, m.focal_spread, m.illumination_angle, m.n_focal)
+        return wp.image(slices, self.slice_thickness, m.electron_dose, m.cs_mm, defocus, m.aperture)
 
     def _geometry(self, mol: atm.AtomList):
         """Centralize, group by element and size the slice stack (pot.py:29-48)."""
@@ -136,7 +144,7 @@ class Pipe:
         their own CUDA streams.  ``to_host``: return numpy images, copied with one
         transfer per group.  ``rois``: a lateral size (int or (n1, n2)) per molecule in
         place of the pipe's roi."""
-        if self.add_water:
+        if self.add_water or self.microscope.partially_coherent:
             imgs = self._run_batch_host(mols, defocus)
             return [im.get() for im in imgs] if to_host else imgs
         m = self.microscope
@@ -220,8 +228,16 @@ class Pipe:
         return out
 
     def _run_batch_host(self, mols, defocus=None) -> List:
-        """run_batch with the front-end on the host (voxel water needs the histograms)."""
+        """run_batch with the front-end on the host (voxel water needs the histograms) or
+        one image at a time (partial coherence)."""
         m = self.microscope
+        if m.partially_coherent:
+            out = []
+            for i, mol in enumerate(mols):
+                s = self.build_slices(mol)
+                wp = self._propagator(s.shape[-2:])
+                out.append(self._form_image(wp, s, m.defocus if defocus is None else defocus[i]))
+            return out
         out: List = [None] * len(mols)
         groups = defaultdict(list)
         built = {}

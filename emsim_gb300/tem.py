@@ -57,12 +57,26 @@ def band_limit_specimen(specimen: Specimen) -> Specimen:
 
 
 class TEM:
-    def __init__(self, electron_dose: float, beam_energy_kev: float, cs_mm: float, defocus: float, aperture: float):
+    """Microscope parameters (tem.py).  Extension: ``focal_spread`` (standard deviation of
+    the defocus, A) and ``illumination_angle`` (semi-angle, rad) make images partially
+    coherent (focal spread as an incoherent sum over ``n_focal`` Gauss-Hermite defocus
+    values, illumination as the quasi-coherent spatial envelope); both 0 by default, which
+    is the reference's coherent imaging."""
+
+    def __init__(self, electron_dose: float, beam_energy_kev: float, cs_mm: float, defocus: float, aperture: float,
+                 focal_spread: float = 0.0, illumination_angle: float = 0.0, n_focal: int = 7):
         self.electron_dose = electron_dose
         self.beam_energy_kev = beam_energy_kev
         self.cs_mm = cs_mm
         self.defocus = defocus
         self.aperture = aperture
+        self.focal_spread = focal_spread
+        self.illumination_angle = illumination_angle
+        self.n_focal = n_focal
+
+    @property
+    def partially_coherent(self) -> bool:
+        return self.focal_spread > 0 or self.illumination_angle > 0
 
     @property
     def relativity_gamma(self):

@@ -94,6 +94,19 @@ int emsim_gb300_multislice_propagate(emsim_gb300_wave_plan* plan, const void* wa
 int emsim_gb300_lens_propagate(emsim_gb300_wave_plan* plan, const void* wave, double cs_mm, double defocus,
                                double aperture, void* wave_out, int n_batch, void* stream);
 
+/* Partially coherent image (no counterpart in the reference, whose README lists the
+ * partially coherent CTF as future work): for each exit wave b,
+ *   image_out[b] = sum_k weights[k] * |IFFT(H_k * E_s * aperture * FFT(psi_b)) / N|^2
+ * with H_k = exp(-i chi) at defocus[k] (focal spread as an incoherent sum over defocus
+ * values, e.g. Gauss-Hermite nodes) and E_s = exp(-(pi a / lambda)^2 |grad chi / 2 pi|^2)
+ * the quasi-coherent envelope of an illumination semi-angle a (rad; 0 = coherent).
+ * work: lens_incoherent_workspace_size(plan, n_batch) bytes of device memory. */
+size_t emsim_gb300_lens_incoherent_workspace_size(const emsim_gb300_wave_plan* plan, int n_batch);
+int emsim_gb300_lens_intensity_incoherent(emsim_gb300_wave_plan* plan, const void* exit_wave, int n_batch,
+                                          double cs_mm, const double* defocus, const double* weights,
+                                          int n_defocus, double illumination_angle, double aperture,
+                                          float* image_out, void* work, size_t work_bytes, void* stream);
+
 /* |psi|^2 (pipe.py:81-82). n = number of complex elements. */
 int emsim_gb300_intensity(const void* wave, float* intensity_out, long long n, void* stream);
 
