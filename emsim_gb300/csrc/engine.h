@@ -116,6 +116,14 @@ int row_tile(int n2);
 int col_tile(int n1);
 
 // generic (any n1, n2) path: direct DFT along rows / columns + element-wise kernels
+// Bluestein line DFTs (bluestein.cu) for lengths n >= 3 that are not powers of two with
+// 2n - 1 <= 4096: return false when they do not apply, else run and put the status in
+// *status.  bluestein_prepare builds the chirp tables of a length ahead of use.
+int bluestein_prepare(int n);
+bool bluestein_rows(const float2* in, float2* out, int n_rows, int n, bool inverse, int n_img, cudaStream_t st,
+                    int* status);
+bool bluestein_cols(float2* data, int n_rows, int n_cols, bool inverse, int n_img, cudaStream_t st, int* status);
+
 int generic_dft_rows(const float2* in, float2* out, int n_rows, int n, bool inverse, const float2* tw_n,
                      int n_img, cudaStream_t st);
 int generic_dft_cols(float2* data, int n_rows, int n_cols, bool inverse, const float2* tw_n, int n_img,

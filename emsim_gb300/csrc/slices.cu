@@ -289,6 +289,9 @@ int emsim_gb300_slice_plan_create(const float* sf_half, int n_elems, int n_slice
     if (!p->fast) {
         if ((st = make_tw(n1, &p->tw1)) != EMSIM_GB300_OK) return fail(st);
         if ((st = make_tw(n2, &p->tw2)) != EMSIM_GB300_OK) return fail(st);
+        // chirp tables of the Bluestein line transforms, built here rather than on first use
+        if ((st = bluestein_prepare(n1)) != EMSIM_GB300_OK) return fail(st);
+        if ((st = bluestein_prepare(n2)) != EMSIM_GB300_OK) return fail(st);
     }
     // T_e(k) = F(k) * SF_e(k) / N on the full spectrum; SF_e(k) = SF_e(-k) supplies the
     // columns beyond n2/2 from the stored half spectrum.

@@ -287,6 +287,8 @@ __global__ void dft_cols_kernel(float2* data, int n_rows, int n_cols, int invers
 
 int generic_dft_rows(const float2* in, float2* out, int n_rows, int n, bool inverse, const float2* tw_n,
                      int n_img, cudaStream_t st) {
+    int status;
+    if (bluestein_rows(in, out, n_rows, n, inverse, n_img, st, &status)) return status;
     const size_t smem = (size_t)n * sizeof(float2);
     EMSIM_TRY(ensure_smem_attr((const void*)dft_rows_kernel, smem));
     dft_rows_kernel<<<dim3(n_rows, n_img), 256, smem, st>>>(in, out, n_rows, n, inverse ? 1 : 0, tw_n,
@@ -297,6 +299,8 @@ int generic_dft_rows(const float2* in, float2* out, int n_rows, int n, bool inve
 
 int generic_dft_cols(float2* data, int n_rows, int n_cols, bool inverse, const float2* tw_n, int n_img,
                      cudaStream_t st) {
+    int status;
+    if (bluestein_cols(data, n_rows, n_cols, inverse, n_img, st, &status)) return status;
     const size_t smem = (size_t)n_rows * sizeof(float2);
     EMSIM_TRY(ensure_smem_attr((const void*)dft_cols_kernel, smem));
     dft_cols_kernel<<<dim3(n_cols, n_img), 256, smem, st>>>(data, n_rows, n_cols, inverse ? 1 : 0, tw_n,

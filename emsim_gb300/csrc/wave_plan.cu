@@ -236,6 +236,9 @@ int emsim_gb300_wave_plan_create(int n1, int n2, double d1, double d2, double wa
     if (!p->fast) {
         if ((st = make_tw(n1, &p->tw1)) != EMSIM_GB300_OK) return fail(st);
         if ((st = make_tw(n2, &p->tw2)) != EMSIM_GB300_OK) return fail(st);
+        // chirp tables of the Bluestein line transforms, built here rather than on first use
+        if ((st = bluestein_prepare(n1)) != EMSIM_GB300_OK) return fail(st);
+        if ((st = bluestein_prepare(n2)) != EMSIM_GB300_OK) return fail(st);
     }
     if (cudaMalloc((void**)&p->prop, prop_slot_bytes(p) * PROP_SLOTS) != cudaSuccess ||
         cudaMalloc((void**)&p->cut, sizeof(int) * n1) != cudaSuccess) {
