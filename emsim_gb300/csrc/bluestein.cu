@@ -10,15 +10,18 @@
 // formed from j^2 mod 2n in integers and FP64, so the tables are accurate for any n.
 //
 // Used by generic_dft_rows / generic_dft_cols for every length n >= 3 with 2n - 1 <= 4096
-// that is not a power of two (others keep the direct DFT).  Each call pads its lines into
-// a stream-ordered scratch buffer (cudaMallocAsync), runs the fast row or column FFT
-// kernels on it, and multiplies back: O(M log M) per line instead of O(n^2).
+// that is not a power of two (others keep the direct DFT).  One kernel per direction does
+// the whole line transform in registers and shared memory: load the line times the
+// chirp, zero-padded to M; forward FFT_M (the fast path's register Stockham FFT); times
+// H; inverse FFT_M; times the chirp, store the first n outputs.  One read and one write
+// of each line, O(M log M) arithmetic instead of O(n^2).
 #include <map>
 #include <mutex>
 #include <string>
 #include <utility>
 
 #include "engine.h"
+#include "wave_passes.cuh"
 
 namespace emsim_gb300 {
 namespace {
@@ -63,79 +66,110 @@ __global__ void chirp_tables_kernel(int n, int M, float2* w, float2* hf, float2*
     }
 }
 
-// rows: lines of length n, contiguous, into lines_p padded lines of length M
-__global__ void pre_rows_kernel(const float2* __restrict__ in, float2* __restrict__ p, long long lines, long long total,
-                                int n, int M, const float2* __restrict__ w, int inverse) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long line = i / M;
-        const int j = (int)(i - line * M);
-        float2 v = make_float2(0.f, 0.f);
-        if (line < lines && j < n) {
-            float2 c = w[j];
-            if (inverse) c.y = -c.y;
-            v = cmul(in[line * n + j], c);
+__device__ __forceinline__ float2 chirp(const float2* __restrict__ w, int j, int inverse) {
+    float2 c = __ldg(w + j);
+    if (inverse) c.y = -c.y;
+    return c;
+}
+
+// B lines of length n per CTA (T = M / 8 threads each, row layout); lines are contiguous
+template <int M>
+__global__ void __launch_bounds__(512) blu_rows_kernel(const float2* in, float2* out, long long lines, int n,
+                                                       const float2* __restrict__ w, const float2* __restrict__ h,
+                                                       int inverse, const float2* __restrict__ tw) {
+    constexpr int T = M / 8;
+    constexpr bool WARP_ONLY = (T <= 32);
+    extern __shared__ float2 sm[];
+    const int B = blockDim.x / T;
+    const int b = threadIdx.x / T;
+    const int t = threadIdx.x - b * T;
+    const long long line = (long long)blockIdx.x * B + b;
+    const bool live = line < lines;
+    float2 v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int j = t + m * T;
+        v[m] = (live && j < n) ? cmul(in[line * n + j], chirp(w, j, inverse)) : make_float2(0.f, 0.f);
+    }
+    fft::fft_regs<M, false, WARP_ONLY>(v, sm, b, t, RowAddr<M>{}, tw);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = cmul(v[m], __ldg(h + t + m * T));
+    fft::fft_regs<M, true, WARP_ONLY>(v, sm, b, t, RowAddr<M>{}, tw);
+    if (live) {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int k = t + m * T;
+            if (k < n) out[line * n + k] = cmul(v[m], chirp(w, k, inverse));
         }
-        p[i] = v;
     }
 }
 
-__global__ void post_rows_kernel(const float2* __restrict__ p, float2* __restrict__ out, long long lines, int n, int M,
-                                 const float2* __restrict__ w, int inverse) {
-    const long long total = lines * n;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long line = i / n;
-        const int k = (int)(i - line * n);
-        float2 c = w[k];
-        if (inverse) c.y = -c.y;
-        out[i] = cmul(p[line * M + k], c);
+// B columns of length n per CTA (column layout, b fastest), in place; the last tile may
+// be partial
+template <int M>
+__global__ void __launch_bounds__(ColThreads<M>::MAX) blu_cols_kernel(float2* data, int n, int n_cols,
+                                                                      long long img_stride,
+                                                                      const float2* __restrict__ w,
+                                                                      const float2* __restrict__ h, int inverse,
+                                                                      const float2* __restrict__ tw) {
+    constexpr int T = M / 8;
+    extern __shared__ float2 sm[];
+    const int B = blockDim.x / T;
+    const int b = threadIdx.x & (B - 1);
+    const int t = threadIdx.x / B;
+    const int col = blockIdx.x * B + b;
+    const bool live = col < n_cols;
+    float2* base = data + blockIdx.y * img_stride + col;
+    const long long ld = n_cols;
+    ColAddrRt addr{B};
+    float2 v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int j = t + m * T;
+        v[m] = (live && j < n) ? cmul(base[j * ld], chirp(w, j, inverse)) : make_float2(0.f, 0.f);
     }
-}
-
-// multiply element (.., j, ..) of every padded line by H[j]; stride = distance between
-// consecutive j (1 for rows, n_cols_p for columns)
-__global__ void mul_kernel(float2* __restrict__ p, long long total, int M, long long stride,
-                           const float2* __restrict__ h) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)((i / stride) % M);
-        p[i] = cmul(p[i], h[j]);
-    }
-}
-
-// columns: (n_img, n, n_cols) into (n_img, M, n_cols_p)
-__global__ void pre_cols_kernel(const float2* __restrict__ in, float2* __restrict__ p, long long total, int n, int M,
-                                int n_cols, int n_cols_p, const float2* __restrict__ w, int inverse) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long img = i / ((long long)M * n_cols_p);
-        const long long rem = i - img * M * n_cols_p;
-        const int j = (int)(rem / n_cols_p);
-        const int c = (int)(rem - (long long)j * n_cols_p);
-        float2 v = make_float2(0.f, 0.f);
-        if (j < n && c < n_cols) {
-            float2 f = w[j];
-            if (inverse) f.y = -f.y;
-            v = cmul(in[(img * n + j) * n_cols + c], f);
+    fft::fft_regs<M, false, false>(v, sm, b, t, addr, tw);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = cmul(v[m], __ldg(h + t + m * T));
+    fft::fft_regs<M, true, false>(v, sm, b, t, addr, tw);
+    if (live) {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int k = t + m * T;
+            if (k < n) base[k * ld] = cmul(v[m], chirp(w, k, inverse));
         }
-        p[i] = v;
     }
 }
 
-__global__ void post_cols_kernel(const float2* __restrict__ p, float2* __restrict__ out, long long total, int n, int M,
-                                 int n_cols, int n_cols_p, const float2* __restrict__ w, int inverse) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long img = i / ((long long)n * n_cols);
-        const long long rem = i - img * n * n_cols;
-        const int k = (int)(rem / n_cols);
-        const int c = (int)(rem - (long long)k * n_cols);
-        float2 f = w[k];
-        if (inverse) f.y = -f.y;
-        out[i] = cmul(p[(img * M + k) * n_cols_p + c], f);
-    }
+template <int M>
+int blu_rows_n(const float2* in, float2* out, long long lines, int n, const float2* w, const float2* h, bool inverse,
+               cudaStream_t st) {
+    constexpr int T = M / 8;
+    const int threads = T > 256 ? T : 256;
+    const int B = threads / T;
+    const size_t smem = (size_t)fft::RowLayout<M>::words(B) * sizeof(float2);
+    EMSIM_TRY(ensure_smem_attr((const void*)blu_rows_kernel<M>, smem));
+    const long long grid = (lines + B - 1) / B;
+    EMSIM_REQUIRE(grid <= 0x7fffffffLL, EMSIM_GB300_ERR_UNSUPPORTED, "bluestein rows: too many lines");
+    blu_rows_kernel<M><<<(unsigned)grid, threads, smem, st>>>(in, out, lines, n, w, h, inverse ? 1 : 0,
+                                                             twiddle_table());
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
 }
 
-int grid_for_total(long long total) {
-    long long b = (total + 255) / 256;
-    if (b > 8192) b = 8192;
-    return b < 1 ? 1 : (int)b;
+template <int M>
+int blu_cols_n(float2* data, int n, int n_cols, int n_img, const float2* w, const float2* h, bool inverse,
+               cudaStream_t st) {
+    constexpr int T = M / 8;
+    int B = ColThreads<M>::MAX / T;
+    if (B > 64) B = 64;
+    while (B > 1 && B / 2 >= n_cols) B >>= 1;  // a power of two, not far above n_cols
+    const size_t smem = (size_t)(M + M / 8) * B * sizeof(float2);
+    EMSIM_TRY(ensure_smem_attr((const void*)blu_cols_kernel<M>, smem));
+    blu_cols_kernel<M><<<dim3((n_cols + B - 1) / B, n_img), B * T, smem, st>>>(
+        data, n, n_cols, (long long)n * n_cols, w, h, inverse ? 1 : 0, twiddle_table());
+    EMSIM_CHECK_LAUNCH();
+    return EMSIM_GB300_OK;
 }
 
 // the chirp tables of length n on the current device, created on first use (nullptr when
@@ -200,77 +234,31 @@ bool bluestein_rows(const float2* in, float2* out, int n_rows, int n, bool inver
                     int* status) {
     const Chirp* c = chirp_for(n, status);
     if (!c) return *status != EMSIM_GB300_OK;
-    const int M = c->M;
     const long long lines = (long long)n_rows * n_img;
-    long long g = 4096 / M;  // largest row tile of the fast row kernels at length M
-    if (g < 1) g = 1;
-    const long long lines_p = (lines + g - 1) / g * g;
-    float2* p = nullptr;
-    if (cudaMallocAsync((void**)&p, sizeof(float2) * (size_t)(lines_p * M), st) != cudaSuccess) {
-        set_error("bluestein rows: cudaMallocAsync of the scratch lines failed");
-        *status = EMSIM_GB300_ERR_CUDA;
-        return true;
+    const float2* h = inverse ? c->hi : c->hf;
+    switch (c->M) {
+#define EMSIM_CASE(M) \
+    case M: *status = blu_rows_n<M>(in, out, lines, n, c->w, h, inverse, st); return true;
+        EMSIM_FAST_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
     }
-    const long long total = lines_p * M;
-    pre_rows_kernel<<<grid_for_total(total), 256, 0, st>>>(in, p, lines, total, n, M, c->w, inverse ? 1 : 0);
-    RowArgs r;
-    r.in = p;
-    r.out = p;
-    r.in_img_stride = r.out_img_stride = total;
-    r.n_rows = (int)lines_p;
-    r.tw = twiddle_table();
-    r.err = error_word();
-    int s = cudaGetLastError() == cudaSuccess ? launch_row(M, ROW_FFT, r, 1, st) : EMSIM_GB300_ERR_CUDA;
-    if (s == EMSIM_GB300_OK) {
-        mul_kernel<<<grid_for_total(total), 256, 0, st>>>(p, total, M, 1, inverse ? c->hi : c->hf);
-        s = cudaGetLastError() == cudaSuccess ? launch_row(M, ROW_IFFT, r, 1, st) : EMSIM_GB300_ERR_CUDA;
-    }
-    if (s == EMSIM_GB300_OK) {
-        post_rows_kernel<<<grid_for_total(lines * n), 256, 0, st>>>(p, out, lines, n, M, c->w, inverse ? 1 : 0);
-        if (cudaGetLastError() != cudaSuccess) s = EMSIM_GB300_ERR_CUDA;
-    }
-    cudaFreeAsync(p, st);
-    if (s != EMSIM_GB300_OK) set_error("bluestein rows: launch failed");
-    *status = s;
+    set_error("bluestein rows: padded length not on the fast path");
+    *status = EMSIM_GB300_ERR_UNSUPPORTED;
     return true;
 }
 
 bool bluestein_cols(float2* data, int n_rows, int n_cols, bool inverse, int n_img, cudaStream_t st, int* status) {
     const Chirp* c = chirp_for(n_rows, status);
     if (!c) return *status != EMSIM_GB300_OK;
-    const int M = c->M, n = n_rows;
-    // column tiles of the fast column kernels are powers of two up to 64 columns
-    const int n_cols_p = n_cols < 64 ? next_pow2(n_cols) : (n_cols + 63) / 64 * 64;
-    const long long total = (long long)n_img * M * n_cols_p;
-    float2* p = nullptr;
-    if (cudaMallocAsync((void**)&p, sizeof(float2) * (size_t)total, st) != cudaSuccess) {
-        set_error("bluestein cols: cudaMallocAsync of the scratch columns failed");
-        *status = EMSIM_GB300_ERR_CUDA;
-        return true;
+    const float2* h = inverse ? c->hi : c->hf;
+    switch (c->M) {
+#define EMSIM_CASE(M) \
+    case M: *status = blu_cols_n<M>(data, n_rows, n_cols, n_img, c->w, h, inverse, st); return true;
+        EMSIM_FAST_SIZES(EMSIM_CASE)
+#undef EMSIM_CASE
     }
-    pre_cols_kernel<<<grid_for_total(total), 256, 0, st>>>(data, p, total, n, M, n_cols, n_cols_p, c->w,
-                                                           inverse ? 1 : 0);
-    ColArgs a;
-    a.data = p;
-    a.img_stride = (long long)M * n_cols_p;
-    a.n_rows = M;
-    a.n_cols = n_cols_p;
-    a.tw = twiddle_table();
-    a.err = error_word();
-    int s = cudaGetLastError() == cudaSuccess ? launch_col(M, COL_FWD, a, n_img, st) : EMSIM_GB300_ERR_CUDA;
-    if (s == EMSIM_GB300_OK) {
-        mul_kernel<<<grid_for_total(total), 256, 0, st>>>(p, total, M, n_cols_p, inverse ? c->hi : c->hf);
-        s = cudaGetLastError() == cudaSuccess ? launch_col(M, COL_INV, a, n_img, st) : EMSIM_GB300_ERR_CUDA;
-    }
-    if (s == EMSIM_GB300_OK) {
-        const long long t2 = (long long)n_img * n * n_cols;
-        post_cols_kernel<<<grid_for_total(t2), 256, 0, st>>>(p, data, t2, n, M, n_cols, n_cols_p, c->w,
-                                                             inverse ? 1 : 0);
-        if (cudaGetLastError() != cudaSuccess) s = EMSIM_GB300_ERR_CUDA;
-    }
-    cudaFreeAsync(p, st);
-    if (s != EMSIM_GB300_OK) set_error("bluestein cols: launch failed");
-    *status = s;
+    set_error("bluestein cols: padded length not on the fast path");
+    *status = EMSIM_GB300_ERR_UNSUPPORTED;
     return true;
 }
 

@@ -116,6 +116,9 @@ int row_tile(int n2);
 int col_tile(int n1);
 
 // generic (any n1, n2) path: direct DFT along rows / columns + element-wise kernels
+// the power-of-two lengths of the fast path, for switch-case instantiation
+#define EMSIM_FAST_SIZES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
+
 // Bluestein line DFTs (bluestein.cu) for lengths n >= 3 that are not powers of two with
 // 2n - 1 <= 4096: return false when they do not apply, else run and put the status in
 // *status.  bluestein_prepare builds the chirp tables of a length ahead of use.

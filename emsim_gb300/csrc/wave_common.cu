@@ -155,7 +155,6 @@ int ensure_smem_attr(const void* func, size_t smem_bytes) {
 // ---------------------------------------------------------------------------------
 // fast-path dispatch
 // ---------------------------------------------------------------------------------
-#define EMSIM_FAST_SIZES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 #define EMSIM_DECL(N)                                                                  \
     extern template int launch_row_n<N>(int, const RowArgs&, int, cudaStream_t);       \
     extern template int launch_col_n<N>(int, const ColArgs&, int, cudaStream_t);       \
