@@ -126,8 +126,13 @@ def tune(n1: int, n2: int, batch: Optional[int] = None, n_slices: int = 6, reps:
                 best_col, best_t = (tma, cols), t
     _set_col(n1, *best_col)
     best_row = (g2["row_tma"], g2["row_rows"])
-    for tma in (-1, 0):
-        for rows in _halvings(g2["default_row_rows_tma"] if tma else g2["default_row_rows"], 1):
+    # row kernels: TMA radix-8 (-1), plain radix-8 (0) and, at length 256, TMA radix-16 (2,
+    # 16 rows per tile by default)
+    row_kernels = {-1: g2["default_row_rows_tma"], 0: g2["default_row_rows"]}
+    if n2 == 256:
+        row_kernels[2] = 16
+    for tma, default_rows in row_kernels.items():
+        for rows in _halvings(default_rows, 1):
             _set_row(n2, tma, rows)
             t = _time_steps(wp, wave, slices, reps)
             if t < best_t:

@@ -1,0 +1,106 @@
+// 256-point FFT as two radix-16 Stockham passes, 16 values per thread, 16 threads per
+// sequence: one shared-memory exchange per transform instead of the two of the radix-8
+// form (8 x 8 x 4), and no third pass.
+//
+// Register contract (as fft_regs, with 16 values): thread t of a sequence holds
+// v[m] = x[t + 16 m] on entry and v[m] = X[t + 16 m] on return.  Pass 1 (stride 1) runs
+// the DFT16 of x[t + 16 r] and scatters output r to position 16 t + r; pass 2 (stride 16)
+// gathers positions t + 16 r, applies W256^(r t) and runs the DFT16, whose outputs are
+// X[t + 16 r] in registers.  The 16 threads of a sequence sit in one warp, so warp
+// barriers order the exchange.
+//
+// DFT16 = radix-4 x radix-4 (the same four-step split one level down): four DFT4 over
+// x[q + 4 n], twiddles W16^(q s), four DFT4 over q.
+#pragma once
+
+#include "fft.cuh"
+
+namespace emsim_gb300 {
+namespace fft16 {
+
+constexpr int N = 256;
+constexpr int T = 16;
+
+// slot of element p of sequence b: the low four bits are XORed with the 16-element block
+// index, so the pass-1 scatter (16 t + r over t) and the pass-2 gather (t + 16 r over t)
+// each touch 16 different bank pairs
+__device__ __forceinline__ int slot(int b, int p) { return b * N + (p ^ ((p >> 4) & 15)); }
+
+// x * W16^k for the constant k of the DFT16 inner twiddles (forward W16 = exp(-2 pi i / 16))
+template <bool INV, int K>
+__device__ __forceinline__ float2 w16(float2 x) {
+    constexpr float C1 = 0.92387953251128675613f;  // cos(pi / 8)
+    constexpr float S1 = 0.38268343236508977173f;  // sin(pi / 8)
+    constexpr float R2 = 0.70710678118654752440f;  // cos(pi / 4)
+    const float sg = INV ? -1.f : 1.f;             // the inverse uses conj(W)
+    switch (K) {
+        case 0: return x;
+        case 1: return cmul(x, make_float2(C1, -sg * S1));
+        case 2: return make_float2(R2 * (x.x + sg * x.y), R2 * (x.y - sg * x.x));
+        case 3: return cmul(x, make_float2(S1, -sg * C1));
+        case 4: return cmul_mi<INV>(x);
+        case 6: return make_float2(R2 * (sg * x.y - x.x), -R2 * (x.y + sg * x.x));
+        case 9: return cmul(x, make_float2(-C1, sg * S1));
+        default: return x;
+    }
+}
+
+// natural-order DFT16 of x[0..15] in place
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 (&x)[16]) {
+    // level 1: DFT4 over n of x[q + 4 n]; output s lands in x[q + 4 s]
+#pragma unroll
+    for (int q = 0; q < 4; ++q) fft::dft4<INV>(x[q], x[q + 4], x[q + 8], x[q + 12]);
+    // inner twiddles W16^(q s) on x[q + 4 s]
+    x[1 + 4 * 1] = w16<INV, 1>(x[1 + 4 * 1]);
+    x[1 + 4 * 2] = w16<INV, 2>(x[1 + 4 * 2]);
+    x[1 + 4 * 3] = w16<INV, 3>(x[1 + 4 * 3]);
+    x[2 + 4 * 1] = w16<INV, 2>(x[2 + 4 * 1]);
+    x[2 + 4 * 2] = w16<INV, 4>(x[2 + 4 * 2]);
+    x[2 + 4 * 3] = w16<INV, 6>(x[2 + 4 * 3]);
+    x[3 + 4 * 1] = w16<INV, 3>(x[3 + 4 * 1]);
+    x[3 + 4 * 2] = w16<INV, 6>(x[3 + 4 * 2]);
+    x[3 + 4 * 3] = w16<INV, 9>(x[3 + 4 * 3]);
+    // level 2: DFT4 over q of x[q + 4 s]; output u lands in x[u + 4 s] = X[s + 4 u]
+#pragma unroll
+    for (int s = 0; s < 4; ++s) fft::dft4<INV>(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
+    // X[s + 4 u] is in x[u + 4 s]: transpose the 4 x 4 index (register renaming)
+    float2 y[16];
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) y[s + 4 * u] = x[u + 4 * s];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = y[i];
+}
+
+// the 256-point transform of the register-held sequence (see the contract above);
+// sm: at least 256 float2 per sequence b; tw: the device table exp(-2 pi i m / 4096)
+template <bool INV, bool TW_SMEM = false>
+__device__ __forceinline__ void fft256(float2 (&v)[16], float2* __restrict__ sm, int b, int t,
+                                       const float2* __restrict__ tw) {
+    // pass 1: stride 1
+    dft16<INV>(v);
+    __syncwarp();  // the previous use of the exchange slots is over
+#pragma unroll
+    for (int r = 0; r < 16; ++r) sm[slot(b, 16 * t + r)] = v[r];
+    __syncwarp();
+    // pass 2: stride 16, twiddles W256^(r t)
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = sm[slot(b, t + 16 * r)];
+    const float2 w1 = fft::twiddle<INV, TW_SMEM>(tw, t * (fft::TW_SIZE / N));
+    const float2 w2 = cmul(w1, w1);
+    const float2 w4 = cmul(w2, w2);
+    const float2 w8 = cmul(w4, w4);
+    const float2 w3 = cmul(w2, w1);
+    float2 w[8] = {make_float2(1.f, 0.f), w1, w2, w3, w4, cmul(w4, w1), cmul(w4, w2), cmul(w4, w3)};
+#pragma unroll
+    for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[r]);
+    v[8] = cmul(v[8], w8);
+#pragma unroll
+    for (int r = 1; r < 8; ++r) v[8 + r] = cmul(v[8 + r], cmul(w8, w[r]));
+    dft16<INV>(v);
+}
+
+}  // namespace fft16
+}  // namespace emsim_gb300

@@ -163,7 +163,6 @@ int ensure_smem_attr(const void* func, size_t smem_bytes) {
 EMSIM_FAST_SIZES(EMSIM_DECL)
 #undef EMSIM_DECL
 
-static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 // tuning table indexed by log2(n), n = 8 .. 4096
 PassTuning g_tuning[13];
@@ -184,6 +183,8 @@ PassTuning pass_tuning(int n) {
 int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
     int bf16_status;
     if (launch_row_bf16(n2, ops, a, n_img, st, &bf16_status)) return bf16_status;
+    int r16_status;
+    if (launch_row16(n2, ops, a, n_img, st, &r16_status)) return r16_status;
     // the adjoint's extra operands (ROW_STORE_PHI, ROW_GRAD) run on the one-tile-per-CTA kernel
     const bool tma = tma_enabled() && n2 >= 16 && pass_tuning(n2).row_tma != 0 && !(ops & (ROW_STORE_PHI | ROW_GRAD)) &&
                      ((ops & ROW_CONST_IN) || aligned16(a.in)) &&
@@ -467,8 +468,10 @@ extern "C" int emsim_gb300_abi_version(void) { return EMSIM_GB300_ABI_VERSION; }
 extern "C" int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int col_tma, int col_cols) {
     using namespace emsim_gb300;
     EMSIM_REQUIRE(fast_len(n), EMSIM_GB300_ERR_INVALID, "set_pass_tuning: n must be a power of two in [8, 4096]");
-    EMSIM_REQUIRE(row_tma >= -1 && row_tma <= 1 && col_tma >= -1 && col_tma <= 1 && row_rows >= 0 && col_cols >= 0,
-                  EMSIM_GB300_ERR_INVALID, "set_pass_tuning: tma flags in {-1, 0, 1}, tiles >= 0");
+    EMSIM_REQUIRE(row_tma >= -1 && row_tma <= 2 && col_tma >= -1 && col_tma <= 1 && row_rows >= 0 && col_cols >= 0,
+                  EMSIM_GB300_ERR_INVALID,
+                  "set_pass_tuning: row kernel in {-1, 0, 1, 2 (radix-16, length 256)}, column in {-1, 0, 1}, "
+                  "tiles >= 0");
     std::lock_guard<std::mutex> lk(g_tuning_mu);
     PassTuning& t = g_tuning[log2_fast(n)];
     t.row_tma = row_tma == 1 ? -1 : row_tma;

@@ -1,0 +1,157 @@
+// Row pass of length 256 with the radix-16 FFT (fft16.cuh): the persistent, TMA-staged
+// structure of row_tma_kernel (two-stage mbarrier pipeline of bulk copies, the stage being
+// computed doubling as the exchange buffer, bounded waits) with 16 threads and 16 values
+// per row.  Selected for length 256 by the pass tuning (row_tma = 2), which the
+// autotuner sets when it measures faster than the radix-8 kernels.
+#include <string>
+
+#include "fft16.cuh"
+#include "wave_tma.cuh"
+
+namespace emsim_gb300 {
+namespace {
+
+constexpr int N = 256, T = fft16::T;
+constexpr int THREADS = 256;  // B = 16 rows per tile at most
+
+template <int OPS>
+__global__ void __launch_bounds__(THREADS, 2) row16_kernel(RowArgs a, int B, int tiles_per_img, int n_tiles) {
+    constexpr bool LOAD_PSI = !(OPS & ROW_CONST_IN);
+    constexpr bool LOAD_V = (OPS & ROW_TRANSMIT) != 0;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int tid = threadIdx.x;
+    const int b = tid / T;
+    const int t = tid - b * T;
+    const int te = B * N;
+    float2* stage0 = reinterpret_cast<float2*>(smem_raw);
+    float2* stage1 = stage0 + te;
+    float* vst0 = reinterpret_cast<float*>(stage1 + te);
+    float* vst1 = vst0 + (LOAD_V ? te : 0);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(vst1 + (LOAD_V ? te : 0));
+    const uint32_t tx = (LOAD_PSI ? te * 8u : 0u) + (LOAD_V ? te * 4u : 0u);
+
+    auto issue = [&](int tile, int buf) {
+        const int img = tile / tiles_per_img;
+        const long long r0 = (long long)(tile - img * tiles_per_img) * B;
+        tma::mbar_arrive_expect_tx(&bar[buf], tx);
+        if (LOAD_PSI)
+            tma::bulk_g2s(buf ? stage1 : stage0, a.in + img * a.in_img_stride + r0 * N, te * 8u, &bar[buf]);
+        if (LOAD_V)
+            tma::bulk_g2s(buf ? vst1 : vst0, a.slice + img * a.slice_img_stride + r0 * N, te * 4u, &bar[buf]);
+    };
+
+    if (tid == 0) {
+        tma::mbar_init(&bar[0], 1);
+        tma::mbar_init(&bar[1], 1);
+        tma::fence_mbar_init();
+    }
+    __syncthreads();
+    const bool pipelined = tx > 0;
+    if (pipelined && tid == 0) {
+        if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
+        if ((int)(blockIdx.x + gridDim.x) < n_tiles) issue(blockIdx.x + gridDim.x, 1);
+    }
+
+    int it = 0;
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++it) {
+        const int buf = it & 1;
+        float2* stage = buf ? stage1 : stage0;
+        if (pipelined && !tma::mbar_wait(&bar[buf], (it >> 1) & 1)) {
+            if (tid == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
+            tma::mbar_wait(&bar[buf ^ 1], ((it + 1) >> 1) & 1);
+            return;
+        }
+        float2 v[16];
+        float vs[16];
+        if (LOAD_PSI) {
+#pragma unroll
+            for (int m = 0; m < 16; ++m) v[m] = stage[b * N + t + m * T];
+        } else {
+#pragma unroll
+            for (int m = 0; m < 16; ++m) v[m] = a.const_val;
+        }
+        if (LOAD_V) {
+            const float* vsrc = buf ? vst1 : vst0;
+#pragma unroll
+            for (int m = 0; m < 16; ++m) vs[m] = vsrc[b * N + t + m * T];
+        }
+        // the stage is reused as the exchange buffer below (rows stay within their warp)
+        __syncwarp();
+
+        if (OPS & ROW_IFFT) fft16::fft256<true>(v, stage, b, t, a.tw);
+        if (OPS & ROW_TRANSMIT) {
+#pragma unroll
+            for (int m = 0; m < 16; ++m) {
+                float s, c;
+                sincosf(a.sigma * vs[m], &s, &c);
+                v[m] = cmul(v[m], make_float2(c, s));
+            }
+        }
+        if (OPS & ROW_FFT) fft16::fft256<false>(v, stage, b, t, a.tw);
+
+        const int img = tile / tiles_per_img;
+        const long long row = (long long)(tile - img * tiles_per_img) * B + b;
+        if (OPS & ROW_OUT_INTENSITY) {
+            float* dst = a.out_int + img * a.out_int_img_stride + row * N;
+#pragma unroll
+            for (int m = 0; m < 16; ++m) dst[t + m * T] = v[m].x * v[m].x + v[m].y * v[m].y;
+        } else {
+            float2* dst = a.out + img * a.out_img_stride + row * N;
+#pragma unroll
+            for (int m = 0; m < 16; ++m) dst[t + m * T] = v[m];
+        }
+        // refill this stage with the tile two steps ahead once every thread is done with it
+        tma::fence_proxy_async();
+        __syncthreads();
+        if (pipelined && tid == 0 && tile + 2 * (int)gridDim.x < n_tiles) issue(tile + 2 * gridDim.x, buf);
+    }
+}
+
+}  // namespace
+
+// 0 when the call is not for this kernel (other length or op combination, unaligned
+// operands), else the launch status in *status
+bool launch_row16(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st, int* status) {
+    if (n2 != N || pass_tuning(N).row_tma != 2 || (ops & (ROW_STORE_PHI | ROW_GRAD))) return false;
+    if (!(ops & ROW_CONST_IN) && !aligned16(a.in)) return false;
+    if ((ops & ROW_TRANSMIT) && (!aligned16(a.slice) || (a.slice_img_stride & 3) != 0)) return false;
+    int B = tile_with_hint(THREADS / T, pass_tuning(N).row_rows, 1);
+    if (B > a.n_rows) B = a.n_rows;
+    if (a.n_rows % B != 0) return false;
+    const int threads = B * T;
+    const int tiles_per_img = a.n_rows / B;
+    const int n_tiles = tiles_per_img * n_img;
+    const size_t te = (size_t)B * N;
+    const bool load_v = (ops & ROW_TRANSMIT) != 0;
+    const size_t smem = 2 * te * sizeof(float2) + (load_v ? 2 * te * sizeof(float) : 0) + 2 * sizeof(uint64_t);
+    switch (ops) {
+#define EMSIM_ROW16_CASE(OPS)                                                              \
+    case OPS: {                                                                            \
+        const void* k = (const void*)row16_kernel<OPS>;                                    \
+        *status = ensure_smem_attr(k, smem);                                               \
+        if (*status != EMSIM_GB300_OK) return true;                                        \
+        const int grid = persistent_grid(k, threads, smem, n_tiles);                       \
+        row16_kernel<OPS><<<grid, threads, smem, st>>>(a, B, tiles_per_img, n_tiles);      \
+        break;                                                                             \
+    }
+        EMSIM_ROW16_CASE(ROW_FFT)
+        EMSIM_ROW16_CASE(ROW_IFFT)
+        EMSIM_ROW16_CASE(ROW_TRANSMIT | ROW_FFT)
+        EMSIM_ROW16_CASE(ROW_IFFT | ROW_TRANSMIT | ROW_FFT)
+        EMSIM_ROW16_CASE(ROW_IFFT | ROW_OUT_INTENSITY)
+        EMSIM_ROW16_CASE(ROW_CONST_IN | ROW_TRANSMIT | ROW_FFT)
+#undef EMSIM_ROW16_CASE
+        default:
+            return false;
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(std::string("radix-16 row pass launch: ") + cudaGetErrorString(e));
+        *status = EMSIM_GB300_ERR_CUDA;
+    } else {
+        *status = EMSIM_GB300_OK;
+    }
+    return true;
+}
+
+}  // namespace emsim_gb300
