@@ -118,8 +118,13 @@ def tune(n1: int, n2: int, batch: Optional[int] = None, n_slices: int = 6, reps:
     g1, g2 = get_tuning(n1), get_tuning(n2)
     best_t = float("inf")
     best_col = (g1["col_tma"], g1["col_cols"])
-    for tma in (-1, 0):
-        for cols in _halvings(g1["default_col_cols_tma"] if tma else g1["default_col_cols"], 2 if tma else 1):
+    # column kernels: TMA radix-8 (-1), plain radix-8 (0) and, at length 256, TMA radix-16
+    # (2, 32 columns per tile by default)
+    col_kernels = {-1: (g1["default_col_cols_tma"], 2), 0: (g1["default_col_cols"], 1)}
+    if n1 == 256:
+        col_kernels[2] = (32, 2)
+    for tma, (default_cols, min_cols) in col_kernels.items():
+        for cols in _halvings(default_cols, min_cols):
             _set_col(n1, tma, cols)
             t = _time_steps(wp, wave, slices, reps)
             if t < best_t:

@@ -101,9 +101,11 @@ PassTuning pass_tuning(int n);
 
 inline bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
-// Radix-16 row pass of length 256 (wave_r16.cu), used when pass_tuning(256).row_tma == 2:
-// false when it does not apply, else launch and put the status in *status.
+// Radix-16 row and column passes of length 256 (wave_r16.cu), used when
+// pass_tuning(256).row_tma / col_tma == 2: false when they do not apply, else launch and
+// put the status in *status.
 bool launch_row16(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st, int* status);
+bool launch_col16(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st, int* status);
 
 // Split-BF16 tensor-core passes (wave_bf16.cu), used when the precision mode is 1 and the
 // call has their shape (length 256; row IFFT|TRANSMIT|FFT, column PROPAGATE).  They

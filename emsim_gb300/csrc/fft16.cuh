@@ -21,10 +21,19 @@ namespace fft16 {
 constexpr int N = 256;
 constexpr int T = 16;
 
-// slot of element p of sequence b: the low four bits are XORed with the 16-element block
-// index, so the pass-1 scatter (16 t + r over t) and the pass-2 gather (t + 16 r over t)
-// each touch 16 different bank pairs
-__device__ __forceinline__ int slot(int b, int p) { return b * N + (p ^ ((p >> 4) & 15)); }
+// Exchange layouts.  Rows (sequence b contiguous, its 16 threads in one warp): the low
+// four bits of p are XORed with the 16-element block index, so the pass-1 scatter
+// (16 t + r over t) and the pass-2 gather (t + 16 r over t) each touch 16 different bank
+// pairs.  Columns (B sequences interleaved, b fastest, as the tile arrives by TMA): with
+// B >= 16 a half-warp touches one position; below that p's low bits are XORed with
+// (p >> 4) & (16 / B - 1), which spreads the 16 / B positions a half-warp touches.
+struct RowSlot {
+    __device__ __forceinline__ int operator()(int b, int p) const { return b * N + (p ^ ((p >> 4) & 15)); }
+};
+struct ColSlot {
+    int B, mask;
+    __device__ __forceinline__ int operator()(int b, int p) const { return (p ^ ((p >> 4) & mask)) * B + b; }
+};
 
 // x * W16^k for the constant k of the DFT16 inner twiddles (forward W16 = exp(-2 pi i / 16))
 template <bool INV, int K>
@@ -74,20 +83,28 @@ __device__ __forceinline__ void dft16(float2 (&x)[16]) {
     for (int i = 0; i < 16; ++i) x[i] = y[i];
 }
 
-// the 256-point transform of the register-held sequence (see the contract above);
-// sm: at least 256 float2 per sequence b; tw: the device table exp(-2 pi i m / 4096)
-template <bool INV, bool TW_SMEM = false>
-__device__ __forceinline__ void fft256(float2 (&v)[16], float2* __restrict__ sm, int b, int t,
+template <bool WARP>
+__device__ __forceinline__ void sync() {
+    if (WARP) __syncwarp();
+    else __syncthreads();
+}
+
+// the 256-point transform of the register-held sequence (see the contract above); all
+// threads of the CTA call it together.  sm: the exchange buffer (256 float2 per sequence,
+// laid out by addr); WARP: a sequence's threads share a warp (rows), else the CTA
+// synchronises (columns); tw: the device table exp(-2 pi i m / 4096)
+template <bool INV, bool WARP, class AddrF, bool TW_SMEM = false>
+__device__ __forceinline__ void fft256(float2 (&v)[16], float2* __restrict__ sm, int b, int t, AddrF addr,
                                        const float2* __restrict__ tw) {
     // pass 1: stride 1
     dft16<INV>(v);
-    __syncwarp();  // the previous use of the exchange slots is over
+    sync<WARP>();  // the previous use of the exchange slots is over
 #pragma unroll
-    for (int r = 0; r < 16; ++r) sm[slot(b, 16 * t + r)] = v[r];
-    __syncwarp();
+    for (int r = 0; r < 16; ++r) sm[addr(b, 16 * t + r)] = v[r];
+    sync<WARP>();
     // pass 2: stride 16, twiddles W256^(r t)
 #pragma unroll
-    for (int r = 0; r < 16; ++r) v[r] = sm[slot(b, t + 16 * r)];
+    for (int r = 0; r < 16; ++r) v[r] = sm[addr(b, t + 16 * r)];
     const float2 w1 = fft::twiddle<INV, TW_SMEM>(tw, t * (fft::TW_SIZE / N));
     const float2 w2 = cmul(w1, w1);
     const float2 w4 = cmul(w2, w2);

@@ -210,6 +210,8 @@ int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
 int launch_col(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st) {
     int bf16_status;
     if (launch_col_bf16(n1, mode, a, n_img, st, &bf16_status)) return bf16_status;
+    int r16_status;
+    if (launch_col16(n1, mode, a, n_img, st, &r16_status)) return r16_status;
     const bool tma = tma_enabled() && n1 >= 16 && pass_tuning(n1).col_tma != 0 && col_tma_B(n1, a.n_cols) >= 2 &&
                      aligned16(a.data);
     if (tma) {
@@ -468,10 +470,9 @@ extern "C" int emsim_gb300_abi_version(void) { return EMSIM_GB300_ABI_VERSION; }
 extern "C" int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int col_tma, int col_cols) {
     using namespace emsim_gb300;
     EMSIM_REQUIRE(fast_len(n), EMSIM_GB300_ERR_INVALID, "set_pass_tuning: n must be a power of two in [8, 4096]");
-    EMSIM_REQUIRE(row_tma >= -1 && row_tma <= 2 && col_tma >= -1 && col_tma <= 1 && row_rows >= 0 && col_cols >= 0,
+    EMSIM_REQUIRE(row_tma >= -1 && row_tma <= 2 && col_tma >= -1 && col_tma <= 2 && row_rows >= 0 && col_cols >= 0,
                   EMSIM_GB300_ERR_INVALID,
-                  "set_pass_tuning: row kernel in {-1, 0, 1, 2 (radix-16, length 256)}, column in {-1, 0, 1}, "
-                  "tiles >= 0");
+                  "set_pass_tuning: row and column kernels in {-1, 0, 1, 2 (radix-16, length 256)}, tiles >= 0");
     std::lock_guard<std::mutex> lk(g_tuning_mu);
     PassTuning& t = g_tuning[log2_fast(n)];
     t.row_tma = row_tma == 1 ? -1 : row_tma;

@@ -206,7 +206,7 @@ def test_pass_tuning_table_host_side():
     assert lib.emsim_gb300_set_pass_tuning(256, -1, 0, -1, 0) == 0
     assert lib.emsim_gb300_set_pass_tuning(100, -1, 0, -1, 0) == 1  # not a power of two
     assert lib.emsim_gb300_set_pass_tuning(256, 3, 0, -1, 0) == 1  # row kernels: -1, 0, 1, 2 (radix 16)
-    assert lib.emsim_gb300_set_pass_tuning(256, -1, 0, 2, 0) == 1  # column kernels: -1, 0, 1
+    assert lib.emsim_gb300_set_pass_tuning(256, -1, 0, 3, 0) == 1  # column kernels: -1, 0, 1, 2 (radix 16)
     assert lib.emsim_gb300_set_pass_tuning(256, 2, 4, -1, 0) == 0
     lib.emsim_gb300_get_pass_tuning(256, out)
     assert list(out)[:2] == [2, 4]
