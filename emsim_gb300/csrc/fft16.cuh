@@ -105,17 +105,18 @@ __device__ __forceinline__ void fft256(float2 (&v)[16], float2* __restrict__ sm,
     // pass 2: stride 16, twiddles W256^(r t)
 #pragma unroll
     for (int r = 0; r < 16; ++r) v[r] = sm[addr(b, t + 16 * r)];
+    // W256^t and W256^(8 t) from the table, the other powers as running products (at most
+    // seven roundings deep), so that only four twiddles are live at a time
     const float2 w1 = fft::twiddle<INV, TW_SMEM>(tw, t * (fft::TW_SIZE / N));
-    const float2 w2 = cmul(w1, w1);
-    const float2 w4 = cmul(w2, w2);
-    const float2 w8 = cmul(w4, w4);
-    const float2 w3 = cmul(w2, w1);
-    float2 w[8] = {make_float2(1.f, 0.f), w1, w2, w3, w4, cmul(w4, w1), cmul(w4, w2), cmul(w4, w3)};
-#pragma unroll
-    for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[r]);
+    const float2 w8 = fft::twiddle<INV, TW_SMEM>(tw, ((8 * t) & (N - 1)) * (fft::TW_SIZE / N));
     v[8] = cmul(v[8], w8);
+    float2 wr = w1;
 #pragma unroll
-    for (int r = 1; r < 8; ++r) v[8 + r] = cmul(v[8 + r], cmul(w8, w[r]));
+    for (int r = 1; r < 8; ++r) {
+        if (r > 1) wr = cmul(wr, w1);
+        v[r] = cmul(v[r], wr);
+        v[8 + r] = cmul(v[8 + r], cmul(w8, wr));
+    }
     dft16<INV>(v);
 }
 
