@@ -15,6 +15,7 @@
 //   C  rows   : W[pair] -> inverse row FFT -> clip(re) -> V[2p], clip(im) -> V[2p+1]
 #pragma once
 
+#include "fft16.cuh"
 #include "slices.h"
 #include "wave_passes.cuh"
 
@@ -237,8 +238,46 @@ template <int N>
 int slice_rows_fwd_n(const SliceArgs& a, cudaStream_t st) {
     return rows_launch<N>(slice_rows_fwd_kernel<N>, a, a.n1, a.n_elems * a.n_pairs, st);
 }
+// length 256: the same pass with the radix-16 FFT (16 threads and values per row)
+__global__ void __launch_bounds__(256) slice_rows_inv16_kernel(SliceArgs a) {
+    constexpr int N = 256, T = fft16::T;
+    extern __shared__ float2 sm[];
+    const int b = threadIdx.x / T;
+    const int t = threadIdx.x - b * T;
+    const int B = blockDim.x / T;
+    const int row = blockIdx.x * B + b;
+    const int y = blockIdx.y;  // img * n_pairs + pair
+    const int img = y / a.n_pairs;
+    const int pair = y - img * a.n_pairs;
+    if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
+    const long long npix = (long long)a.n1 * N;
+    const float2* src = a.work + (long long)y * npix + (long long)row * N;
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = src[t + m * T];
+    fft16::fft256<true, true>(v, sm, b, t, fft16::RowSlot{}, a.tw);
+    const int s0 = 2 * pair, s1 = 2 * pair + 1;
+    float* out = a.out + (long long)img * a.n_slices * npix;
+    float* o0 = out + (long long)s0 * npix + (long long)row * N;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) o0[t + m * T] = clip_low(v[m].x);
+    if (s1 < a.n_slices) {
+        float* o1 = out + (long long)s1 * npix + (long long)row * N;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) o1[t + m * T] = clip_low(v[m].y);
+    }
+}
+
 template <int N>
 int slice_rows_inv_n(const SliceArgs& a, cudaStream_t st) {
+    if (N == 256 && a.n1 % 16 == 0) {
+        const int B = 16;  // rows per CTA, 256 threads
+        const size_t smem = (size_t)B * N * sizeof(float2);
+        EMSIM_TRY(ensure_smem_attr((const void*)slice_rows_inv16_kernel, smem));
+        slice_rows_inv16_kernel<<<dim3(a.n1 / B, a.n_img * a.n_pairs), B * fft16::T, smem, st>>>(a);
+        EMSIM_CHECK_LAUNCH();
+        return EMSIM_GB300_OK;
+    }
     return rows_launch<N>(slice_rows_inv_kernel<N>, a, a.n1, a.n_img * a.n_pairs, st);
 }
 // Pass B on columns of length n1 (= N here)
