@@ -126,6 +126,8 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
         for (int i = threadIdx.x; i <= N; i += blockDim.x) s_off[i] = __ldg(off_g + i);
         __syncthreads();
         const unsigned base = s_off[0], count = s_off[N] - base;
+        // an element without atoms in this slice pair adds exactly zero: skip its transform
+        if (count == 0) continue;
         const bool cached = count <= (unsigned)ITEM_CACHE;
         if (cached)
             for (unsigned i = threadIdx.x; i < count; i += blockDim.x) s_items[i] = __ldg(a.items + base + i);
