@@ -172,6 +172,10 @@ __global__ void __launch_bounds__(COL_THREADS, 1)
     float2* stage0 = reinterpret_cast<float2*>(smem_raw);
     float2* stage1 = stage0 + te;
     uint64_t* bar = reinterpret_cast<uint64_t*>(stage1 + te);
+    // propagate: the row factors p1 (the same for every tile) staged once in shared memory
+    float4* s_p1 = reinterpret_cast<float4*>(bar + 2);
+    if (MODE == COL_PROPAGATE)
+        for (int i = threadIdx.x; i < N; i += blockDim.x) s_p1[i] = __ldg(a.p1 + i);
     const fft16::ColSlot addr{B, B >= 16 ? 0 : (16 / B) - 1};
     const int live_per_img = lt_lo + lt_hi;
     const int n_tiles = live_per_img * n_img;
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(COL_THREADS, 1)
             const float2 p2 = __ldg(a.p2 + col);
 #pragma unroll
             for (int m = 0; m < 16; ++m) {
-                const float4 q = __ldg(a.p1 + t + m * T);
+                const float4 q = s_p1[t + m * T];
                 v[m] = (k2a <= __float_as_int(q.z)) ? cmul(v[m], cmul(make_float2(q.x, q.y), p2))
                                                     : make_float2(0.f, 0.f);
             }
@@ -267,7 +271,7 @@ bool launch_col16(int n1, int mode, const ColArgs& a, int n_img, cudaStream_t st
     const int threads = B * T;
     const int tiles_per_img = a.n_cols / B;
     const LiveTiles lt = mode == COL_PROPAGATE ? live_tiles(a, B, tiles_per_img) : LiveTiles{tiles_per_img, 0};
-    const size_t smem = 2 * (size_t)N * B * sizeof(float2) + 2 * sizeof(uint64_t);
+    const size_t smem = 2 * (size_t)N * B * sizeof(float2) + 2 * sizeof(uint64_t) + N * sizeof(float4);
     CUtensorMap map;
     *status = make_col_tensor_map(&map, a.data, (long long)n_img * N, a.n_cols, B, ColTma<N>::BOXR);
     if (*status != EMSIM_GB300_OK) return true;
