@@ -19,6 +19,12 @@ from . import atoms as atm
 from . import backend, pot, tem, wave
 
 
+# chunked run_batch: at least this many molecules and atoms per chunk, at most _MAX_CHUNKS
+_CHUNK_MIN_MOLS = 64
+_CHUNK_MIN_ATOMS = 1 << 21
+_MAX_CHUNKS = 2
+
+
 def _fast_len(n: int) -> bool:
     return 8 <= n <= 4096 and (n & (n - 1)) == 0
 
@@ -147,12 +153,69 @@ class Pipe:
         if self.add_water or self.microscope.partially_coherent:
             imgs = self._run_batch_host(mols, defocus)
             return [im.get() for im in imgs] if to_host else imgs
-        m = self.microscope
-        dev = backend._device()
         sizes = [len(mol.elements) for mol in mols]
         if any(s == 0 for s in sizes):
             raise ValueError("zero-size array to reduction operation minimum which has no identity")
         nm = len(mols)
+        # Large batches (128 molecules and more) run in two chunks, each on its own stream:
+        # while the GPU builds and images the first, the host stages the second and its
+        # front-end (H2D, centralisation, the sync that sizes the stacks) runs beside it.
+        # Images are independent, so the results do not depend on the chunking.
+        n_chunks = 1
+        if nm >= 2 * _CHUNK_MIN_MOLS and sum(sizes) >= 2 * _CHUNK_MIN_ATOMS:
+            n_chunks = int(min(_MAX_CHUNKS, nm // _CHUNK_MIN_MOLS, sum(sizes) // _CHUNK_MIN_ATOMS))
+        bounds = np.linspace(0, nm, n_chunks + 1).round().astype(int)
+        main = torch.cuda.current_stream()
+        done = []
+        streams = []
+        for c in range(n_chunks):
+            a, b = int(bounds[c]), int(bounds[c + 1])
+            st = main if n_chunks == 1 else self._chunk_stream(c)
+            if st is not main:
+                st.wait_stream(main)
+                streams.append(st)
+            with torch.cuda.stream(st):
+                part = self._launch_chunk(mols[a:b], None if defocus is None else defocus[a:b],
+                                          None if rois is None else rois[a:b])
+                for idx, imgs in part:
+                    if st is not main:
+                        imgs.record_stream(main)
+                    done.append(([a + i for i in idx], imgs))
+        for st in streams:
+            main.wait_stream(st)
+        if to_host:
+            # one transfer per group into page-locked memory from torch's caching host
+            # allocator (a pageable copy of 33 MB takes ~2.4 ms against ~0.2 ms); each
+            # returned array keeps its buffer alive
+            pinned = []
+            for idx, imgs in done:
+                h = torch.empty(imgs.shape, dtype=imgs.dtype, pin_memory=True)
+                h.copy_(imgs, non_blocking=True)
+                pinned.append(h)
+            main.synchronize()
+            done = [(idx, h.numpy()) for (idx, _), h in zip(done, pinned)]
+        out: List = [None] * nm
+        for idx, imgs in done:
+            for j, i in enumerate(idx):
+                out[i] = imgs[j]
+        return out
+
+    def _chunk_stream(self, c: int):
+        pool = getattr(self, "_streams", None)
+        if pool is None:
+            pool = self._streams = {}
+        dev = torch.cuda.current_device()
+        if (dev, c) not in pool:
+            pool[(dev, c)] = torch.cuda.Stream()
+        return pool[(dev, c)]
+
+    def _launch_chunk(self, mols, defocus, rois):
+        """Queue the device work of one chunk on the current stream (groups of other
+        lateral sizes on side streams joined back into it); returns [(indices, images)]."""
+        m = self.microscope
+        dev = backend._device()
+        nm = len(mols)
+        sizes = [len(mol.elements) for mol in mols]
         offsets = np.zeros(nm + 1, dtype=np.int64)
         offsets[1:] = np.cumsum(sizes)
         n_atoms = int(offsets[-1])
@@ -181,7 +244,6 @@ class Pipe:
             n_sl[i] = ns
             fast = _fast_len(n1) and _fast_len(n2)
             groups[(n1, n2) if fast else (ns, n1, n2)].append(i)
-        out: List = [None] * nm
         main = torch.cuda.current_stream()
         ready = torch.cuda.Event()
         ready.record(main)
@@ -220,21 +282,7 @@ class Pipe:
             done.append((idx, imgs))
         for st in side:
             main.wait_stream(st)
-        if to_host:
-            # one transfer per group into page-locked memory from torch's caching host
-            # allocator (a pageable copy of 33 MB takes ~2.4 ms against ~0.2 ms); each
-            # returned array keeps its buffer alive
-            pinned = []
-            for idx, imgs in done:
-                h = torch.empty(imgs.shape, dtype=imgs.dtype, pin_memory=True)
-                h.copy_(imgs, non_blocking=True)
-                pinned.append(h)
-            main.synchronize()
-            done = [(idx, h.numpy()) for (idx, _), h in zip(done, pinned)]
-        for idx, imgs in done:
-            for j, i in enumerate(idx):
-                out[i] = imgs[j]
-        return out
+        return done
 
     def _run_batch_host(self, mols, defocus=None) -> List:
         """run_batch with the front-end on the host (voxel water needs the histograms) or

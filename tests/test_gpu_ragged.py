@@ -100,3 +100,18 @@ def test_mixed_lateral_sizes_on_streams(eng):
     for k, mol in enumerate(mols):
         alone = np.asarray(p.run_batch([mol])[0].get())
         np.testing.assert_array_equal(imgs[k], alone)
+
+
+def test_large_batch_runs_in_chunks_equal_single(eng):
+    """128 molecules of 35k atoms (4.5 M atoms) run as two chunks on two streams; every
+    image equals the one its molecule gets alone, bitwise."""
+    torch, atoms, backend, pipe, tem = eng
+    from emsim_gb300 import synth
+    m = tem.TEM(electron_dose=20.0, beam_energy_kev=200.0, cs_mm=1.3, defocus=700.0, aperture=10e-3)
+    p = pipe.Pipe(m, resolution=2.0, slice_thickness=2.0, roi=128, add_water=False)
+    mols = [atoms.AtomList(*synth.protein_blob(35_000, 30.0 + (i % 5), 500 + i)) for i in range(128)]
+    dfs = [600.0 + 5 * i for i in range(128)]
+    got = p.run_batch(mols, defocus=dfs, to_host=True)
+    for i in (0, 63, 64, 127):
+        one = p.run_batch([mols[i]], defocus=[dfs[i]], to_host=True)[0]
+        np.testing.assert_array_equal(got[i], one)
