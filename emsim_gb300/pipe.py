@@ -157,10 +157,10 @@ class Pipe:
         if any(s == 0 for s in sizes):
             raise ValueError("zero-size array to reduction operation minimum which has no identity")
         nm = len(mols)
-        # Large batches (128 molecules and more) run in two chunks, each on its own stream:
-        # while the GPU builds and images the first, the host stages the second and its
-        # front-end (H2D, centralisation, the sync that sizes the stacks) runs beside it.
-        # Images are independent, so the results do not depend on the chunking.
+        # Large batches (128 molecules and 4 M atoms and more) run in two chunks, each on its
+        # own stream: while the GPU builds and images the first, the host stages the second
+        # and its front-end (H2D, centralisation, the sync that sizes the stacks) runs beside
+        # it.  Images are independent, so the results do not depend on the chunking.
         n_chunks = 1
         if nm >= 2 * _CHUNK_MIN_MOLS and sum(sizes) >= 2 * _CHUNK_MIN_ATOMS:
             n_chunks = int(min(_MAX_CHUNKS, nm // _CHUNK_MIN_MOLS, sum(sizes) // _CHUNK_MIN_ATOMS))
