@@ -651,7 +651,8 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "images/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64 (numpy complex128)", "data": "synthetic (seeded blobs)",
-           "config": {"workload": "blob 50k C/N/O/S atoms r=40A, roi 256, pixel 1A, dz 2A, 40 slices, 200 keV",
+           "config": {"workload": "blob 50k C/N/O/S atoms r=40A, roi 256, pixel 1A, dz 2A, 40 slices, 200 keV, "
+                                  "Cs 1.3 mm, df 700 A, aperture 10 mrad",
                       "parallelism": f"{procs} host processes"},
            "cpu_baseline": {"value": round(v, 4), "unit": "images/s", "cores": procs, "kind": "port",
                             "sample": "reference numpy algorithm (bit-exact oracle restatement; the reference "
