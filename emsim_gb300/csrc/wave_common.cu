@@ -185,8 +185,7 @@ int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
     if (launch_row_bf16(n2, ops, a, n_img, st, &bf16_status)) return bf16_status;
     int r16_status;
     if (launch_row16(n2, ops, a, n_img, st, &r16_status)) return r16_status;
-    // the adjoint's extra operands (ROW_STORE_PHI, ROW_GRAD) run on the one-tile-per-CTA kernel
-    const bool tma = tma_enabled() && n2 >= 16 && pass_tuning(n2).row_tma != 0 && !(ops & (ROW_STORE_PHI | ROW_GRAD)) &&
+    const bool tma = tma_enabled() && n2 >= 16 && pass_tuning(n2).row_tma != 0 &&
                      ((ops & ROW_CONST_IN) || aligned16(a.in)) &&
                      (!(ops & ROW_TRANSMIT) || (aligned16(a.slice) && (a.slice_img_stride & 3) == 0));
     if (tma) {

@@ -96,7 +96,20 @@ __global__ void __launch_bounds__(RowTma<N>::THREADS, RowTma<N>::MIN_BLOCKS)
         // the stage is reused as the (swizzled) exchange buffer below
         fft::tile_sync<WARP_ONLY>();
 
+        const int img = tile / tiles_per_img;
+        const long long row = (long long)(tile - img * tiles_per_img) * B + b;
         if (OPS & ROW_IFFT) fft::fft_regs<N, true, WARP_ONLY>(v, stage, b, t, RowAddr<N>{}, a.tw);
+        if (OPS & ROW_GRAD) {
+            // dL/dV = 2 sigma Im(mu conj(phi)) with mu = v (the back-propagated wave)
+            const float2* ph = a.phi + img * a.phi_img_stride + row * N;
+            float* g = a.grad + img * a.grad_img_stride + row * N;
+            const float s2 = 2.f * a.sigma_grad;
+#pragma unroll
+            for (int m = 0; m < 8; ++m) {
+                const float2 f = ph[t + m * T];
+                g[t + m * T] = s2 * (v[m].y * f.x - v[m].x * f.y);
+            }
+        }
         if (OPS & ROW_TRANSMIT) {
 #pragma unroll
             for (int m = 0; m < 8; ++m) {
@@ -105,10 +118,13 @@ __global__ void __launch_bounds__(RowTma<N>::THREADS, RowTma<N>::MIN_BLOCKS)
                 v[m] = cmul(v[m], make_float2(c, s));
             }
         }
+        if (OPS & ROW_STORE_PHI) {
+            float2* ph = a.phi + img * a.phi_img_stride + row * N;
+#pragma unroll
+            for (int m = 0; m < 8; ++m) ph[t + m * T] = v[m];
+        }
         if (OPS & ROW_FFT) fft::fft_regs<N, false, WARP_ONLY>(v, stage, b, t, RowAddr<N>{}, a.tw);
 
-        const int img = tile / tiles_per_img;
-        const long long row = (long long)(tile - img * tiles_per_img) * B + b;
         if (OPS & ROW_OUT_INTENSITY) {
             float* dst = a.out_int + img * a.out_int_img_stride + row * N;
 #pragma unroll
@@ -278,6 +294,10 @@ int launch_row_tma_n(int ops, const RowArgs& a, int n_img, cudaStream_t st) {
         EMSIM_ROW_TMA_CASE(ROW_IFFT | ROW_TRANSMIT | ROW_FFT)
         EMSIM_ROW_TMA_CASE(ROW_IFFT | ROW_OUT_INTENSITY)
         EMSIM_ROW_TMA_CASE(ROW_CONST_IN | ROW_TRANSMIT | ROW_FFT)
+        EMSIM_ROW_TMA_CASE(ROW_IFFT | ROW_TRANSMIT | ROW_FFT | ROW_STORE_PHI)
+        EMSIM_ROW_TMA_CASE(ROW_CONST_IN | ROW_TRANSMIT | ROW_FFT | ROW_STORE_PHI)
+        EMSIM_ROW_TMA_CASE(ROW_IFFT | ROW_GRAD | ROW_TRANSMIT | ROW_FFT)
+        EMSIM_ROW_TMA_CASE(ROW_IFFT | ROW_GRAD)
 #undef EMSIM_ROW_TMA_CASE
         default:
             set_error("row pass: unsupported op combination");
