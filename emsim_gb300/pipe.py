@@ -153,6 +153,54 @@ class Pipe:
         if self.add_water or self.microscope.partially_coherent:
             imgs = self._run_batch_host(mols, defocus)
             return [im.get() for im in imgs] if to_host else imgs
+        if to_host:
+            return self.submit_batch(mols, defocus, rois).result()
+        done = self._queue_batch(mols, defocus, rois, torch.cuda.current_stream(), 0)
+        out: List = [None] * len(mols)
+        for idx, imgs in done:
+            for j, i in enumerate(idx):
+                out[i] = imgs[j]
+        return out
+
+    def submit_batch(self, mols: Sequence[atm.AtomList], defocus: Optional[Sequence[float]] = None,
+                     rois: Optional[Sequence] = None) -> "PendingImages":
+        """Queue the images of many molecules and their copy to page-locked host memory,
+        and return without waiting for the GPU.  ``result()`` of the returned object gives
+        what ``run_batch(..., to_host=True)`` gives.
+
+        Successive batches alternate between two sets of CUDA streams, so the host side of
+        the next batch (staging its atoms, the H2D copy, the front-end's small sync that
+        sizes the stacks, the launches) runs while the GPU forms this batch's images::
+
+            pending = p.submit_batch(batch0)
+            for nxt in batches[1:]:
+                following = p.submit_batch(nxt)
+                consume(pending.result())
+                pending = following
+            consume(pending.result())
+        """
+        if self.add_water or self.microscope.partially_coherent:
+            return PendingImages.completed([im.get() for im in self._run_batch_host(mols, defocus)])
+        slot = getattr(self, "_slot", 1) ^ 1
+        self._slot = slot
+        base = self._chunk_stream((slot, "base"))
+        base.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(base):
+            done = self._queue_batch(mols, defocus, rois, base, slot)
+            groups = []
+            for idx, imgs in done:
+                # one transfer per group into page-locked memory from torch's caching host
+                # allocator (a pageable copy of 33 MB takes ~2.4 ms against ~0.2 ms)
+                h = torch.empty(imgs.shape, dtype=imgs.dtype, pin_memory=True)
+                h.copy_(imgs, non_blocking=True)
+                groups.append((idx, h, imgs))
+            ev = torch.cuda.Event()
+            ev.record(base)
+        return PendingImages(len(mols), groups, ev)
+
+    def _queue_batch(self, mols, defocus, rois, main, slot) -> List:
+        """Queue a batch's device work so that it completes in stream ``main``; returns
+        [(indices, images)] with images (len(indices), n1, n2) on the device."""
         sizes = [len(mol.elements) for mol in mols]
         if any(s == 0 for s in sizes):
             raise ValueError("zero-size array to reduction operation minimum which has no identity")
@@ -165,12 +213,11 @@ class Pipe:
         if nm >= 2 * _CHUNK_MIN_MOLS and sum(sizes) >= 2 * _CHUNK_MIN_ATOMS:
             n_chunks = int(min(_MAX_CHUNKS, nm // _CHUNK_MIN_MOLS, sum(sizes) // _CHUNK_MIN_ATOMS))
         bounds = np.linspace(0, nm, n_chunks + 1).round().astype(int)
-        main = torch.cuda.current_stream()
         done = []
         streams = []
         for c in range(n_chunks):
             a, b = int(bounds[c]), int(bounds[c + 1])
-            st = main if n_chunks == 1 else self._chunk_stream(c)
+            st = main if n_chunks == 1 else self._chunk_stream((slot, c))
             if st is not main:
                 st.wait_stream(main)
                 streams.append(st)
@@ -183,31 +230,16 @@ class Pipe:
                     done.append(([a + i for i in idx], imgs))
         for st in streams:
             main.wait_stream(st)
-        if to_host:
-            # one transfer per group into page-locked memory from torch's caching host
-            # allocator (a pageable copy of 33 MB takes ~2.4 ms against ~0.2 ms); each
-            # returned array keeps its buffer alive
-            pinned = []
-            for idx, imgs in done:
-                h = torch.empty(imgs.shape, dtype=imgs.dtype, pin_memory=True)
-                h.copy_(imgs, non_blocking=True)
-                pinned.append(h)
-            main.synchronize()
-            done = [(idx, h.numpy()) for (idx, _), h in zip(done, pinned)]
-        out: List = [None] * nm
-        for idx, imgs in done:
-            for j, i in enumerate(idx):
-                out[i] = imgs[j]
-        return out
+        return done
 
-    def _chunk_stream(self, c: int):
+    def _chunk_stream(self, key):
         pool = getattr(self, "_streams", None)
         if pool is None:
             pool = self._streams = {}
         dev = torch.cuda.current_device()
-        if (dev, c) not in pool:
-            pool[(dev, c)] = torch.cuda.Stream()
-        return pool[(dev, c)]
+        if (dev, key) not in pool:
+            pool[(dev, key)] = torch.cuda.Stream()
+        return pool[(dev, key)]
 
     def _launch_chunk(self, mols, defocus, rois):
         """Queue the device work of one chunk on the current stream (groups of other
@@ -314,3 +346,37 @@ class Pipe:
     def __repr__(self):
         return (f"{{ImagePipe | resolution = {self._resolution}Angstrom, slice_thickness = {self.slice_thickness}"
                 f"Angstrom, roi = {self.roi}, add_water = {self.add_water}, microscope = {self.microscope}}}")
+
+
+class PendingImages:
+    """Images of a batch queued by ``Pipe.submit_batch``: the device work and the copy to
+    page-locked host memory are in flight.  ``result()`` waits for them and returns the
+    numpy images in input order (each array keeps its page-locked buffer alive)."""
+
+    def __init__(self, n: int, groups, event):
+        self._n = n
+        self._groups = groups  # [(indices, page-locked host tensor, device tensor)]
+        self._event = event
+        self._out = None
+
+    @classmethod
+    def completed(cls, images: List) -> "PendingImages":
+        p = cls(len(images), None, None)
+        p._out = list(images)
+        return p
+
+    def done(self) -> bool:
+        """True once result() will not wait."""
+        return self._out is not None or self._event.query()
+
+    def result(self) -> List[np.ndarray]:
+        if self._out is None:
+            self._event.synchronize()
+            out: List = [None] * self._n
+            for idx, h, _ in self._groups:
+                a = h.numpy()
+                for j, i in enumerate(idx):
+                    out[i] = a[j]
+            self._out = out
+            self._groups = None
+        return self._out

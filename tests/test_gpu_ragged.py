@@ -115,3 +115,35 @@ def test_large_batch_runs_in_chunks_equal_single(eng):
     for i in (0, 63, 64, 127):
         one = p.run_batch([mols[i]], defocus=[dfs[i]], to_host=True)[0]
         np.testing.assert_array_equal(got[i], one)
+
+
+def test_submitted_batches_in_flight_equal_serial(eng):
+    """Pipe.submit_batch keeps two batches in flight on alternating stream sets (one of
+    them chunked, one with two lateral sizes); each PendingImages.result() equals
+    run_batch(to_host=True) of the same batch, bitwise and in input order, whatever the
+    order the results are collected in."""
+    torch, atoms, backend, pipe, tem = eng
+    from emsim_gb300 import synth
+    m = tem.TEM(electron_dose=20.0, beam_energy_kev=200.0, cs_mm=1.3, defocus=700.0, aperture=10e-3)
+    p = pipe.Pipe(m, resolution=2.0, slice_thickness=2.0, roi=128, add_water=False)
+    big = [atoms.AtomList(*synth.protein_blob(35_000, 30.0 + (i % 5), 900 + i)) for i in range(128)]
+    rng = np.random.default_rng(11)
+    small = [atoms.AtomList(el, xyz) for el, xyz in _mols(rng, [(1500, 8.0, 14.0), (1500, 8.0, 30.0),
+                                                                 (1000, 12.0, 14.0)])]
+    rois = [64, 128, 64]
+    batches = [(big, None), (small, rois), (big[::-1], None), (small[::-1], rois[::-1])]
+    serial = [p.run_batch(mols, to_host=True, rois=r) for mols, r in batches]
+    pend = [p.submit_batch(mols, rois=r) for mols, r in batches[:2]]
+    got = [None] * 4
+    got[1] = pend[1].result()
+    pend.append(p.submit_batch(batches[2][0]))
+    got[0] = pend[0].result()
+    pend.append(p.submit_batch(batches[3][0], rois=batches[3][1]))
+    got[3] = pend[3].result()
+    got[2] = pend[2].result()
+    assert pend[2].done()
+    for g, s in zip(got, serial):
+        assert len(g) == len(s)
+        for a, b in zip(g, s):
+            assert isinstance(a, np.ndarray)
+            np.testing.assert_array_equal(a, b)
