@@ -124,7 +124,7 @@ __global__ void atoms_bucket_kernel(AtomBucketArgs a) {
             const float z = a.coords[3 * r + 0], x = a.coords[3 * r + 1], y = a.coords[3 * r + 2];
             int s, i, j;
             if (bin_axis(z, a.ax0, s) && bin_axis(x, a.ax1, i) && bin_axis(y, a.ax2, j)) {
-                bk = (unsigned)((((long long)lo * a.n_pairs + (s >> 1)) * plane + i) * ROW_SUB + (j & (ROW_SUB - 1)));
+                bk = (unsigned)(((long long)lo * a.n_pairs + (s >> 1)) * plane + i);
                 item = ((unsigned)(s & 1) << 31) | (unsigned)j;
                 atomicAdd(a.bucket_count + bk, 1u);
             }
@@ -174,8 +174,7 @@ __global__ void atoms_bucket_z_kernel(AtomBucketZArgs a) {
             }
             int s, i, j;
             if (bin_axis(z, az, s) && bin_axis(x, a.ax1, i) && bin_axis(y, a.ax2, j)) {
-                bk = (unsigned)(((((long long)slot * a.n_elems + e) * a.n_pairs + (s >> 1)) * plane + i) * ROW_SUB +
-                                (j & (ROW_SUB - 1)));
+                bk = (unsigned)((((long long)slot * a.n_elems + e) * a.n_pairs + (s >> 1)) * plane + i);
                 item = ((unsigned)(s & 1) << 31) | (unsigned)j;
                 atomicAdd(a.bucket_count + bk, 1u);
             }

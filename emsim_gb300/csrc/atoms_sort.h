@@ -1,4 +1,4 @@
-// Counting sort of atoms into (image, element, slice pair, row, column mod 4) buckets.
+// Counting sort of atoms into (image, element, slice pair, row) buckets.
 #pragma once
 
 #include "binning.cuh"
@@ -7,9 +7,6 @@
 namespace emsim_gb300 {
 
 constexpr unsigned INVALID_BUCKET = 0xffffffffu;
-// a row's atoms are bucketed by column index mod ROW_SUB: the slice build's row sums of
-// the columns c + k n2 / 4 (k = 0..3) then follow from one table lookup per atom
-constexpr int ROW_SUB = 4;
 
 struct AtomBucketArgs {
     const float* coords = nullptr;       // (n_atoms, 3) float32, columns (z, x, y)

@@ -146,9 +146,7 @@ const float2* twiddle_table();
 // device address of the error word kernels set when a bounded wait gives up
 int* error_word();
 
-// dynamic shared memory a kernel may be given (bytes); ensure_smem_attr opts a kernel into
-// this limit (once per device) when a launch needs more than the default 48 KB
-constexpr size_t SMEM_ATTR_MAX = 200 * 1024;
+// opt a kernel into more than 48 KB of dynamic shared memory (once per device)
 int ensure_smem_attr(const void* func, size_t smem_bytes);
 
 // element-wise kernels (any size)

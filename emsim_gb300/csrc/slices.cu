@@ -228,7 +228,7 @@ AtomsWorkspace atoms_workspace(const emsim_gb300_slice_plan* p, unsigned n_atoms
     AtomsWorkspace w;
     const long long n_groups = (long long)n_img * p->n_elems;
     const long long pairs = (p->n_slices + 1) / 2;
-    w.n_buckets = n_groups * pairs * p->n1 * ROW_SUB;
+    w.n_buckets = n_groups * pairs * p->n1;
     size_t o = 0;
     auto take = [&](size_t bytes) {
         const size_t at = o;
@@ -375,7 +375,7 @@ int emsim_gb300_build_slices(emsim_gb300_slice_plan* p, const float* coords, uns
     EMSIM_REQUIRE(((uintptr_t)workspace & 255) == 0, EMSIM_GB300_ERR_INVALID,
                   "build_slices: workspace not 256-byte aligned");
     EMSIM_REQUIRE(w.n_buckets < (long long)INVALID_BUCKET, EMSIM_GB300_ERR_UNSUPPORTED,
-                  "build_slices: more than 2^32 - 1 (image, element, slice pair, row, column mod 4) buckets");
+                  "build_slices: more than 2^32 - 1 (image, element, slice pair, row) buckets");
     const long long pairs = (p->n_slices + 1) / 2;
     EMSIM_REQUIRE((long long)n_batch * pairs <= 65535, EMSIM_GB300_ERR_UNSUPPORTED,
                   "build_slices: more than 65535 image x slice-pair planes per call");
@@ -451,7 +451,7 @@ int emsim_gb300_build_slices_ragged(emsim_gb300_slice_plan* p, const float* coor
     EMSIM_REQUIRE(((uintptr_t)workspace & 255) == 0, EMSIM_GB300_ERR_INVALID,
                   "build_slices_z: workspace not 256-byte aligned");
     EMSIM_REQUIRE(w.n_buckets < (long long)INVALID_BUCKET, EMSIM_GB300_ERR_UNSUPPORTED,
-                  "build_slices_z: more than 2^32 - 1 (image, element, slice pair, row, column mod 4) buckets");
+                  "build_slices_z: more than 2^32 - 1 (image, element, slice pair, row) buckets");
     const long long pairs = (p->n_slices + 1) / 2;
     EMSIM_REQUIRE((long long)n_batch * pairs <= 65535, EMSIM_GB300_ERR_UNSUPPORTED,
                   "build_slices_z: more than 65535 image x slice-pair planes per call");

@@ -1,7 +1,6 @@
 // Internal interface of the slice builder (binning + projected-potential slices).
 #pragma once
 
-#include "atoms_sort.h"
 #include "engine.h"
 
 namespace emsim_gb300 {
@@ -15,9 +14,7 @@ struct SliceArgs {
     int n_elems = 0, n_slices = 0, n_pairs = 0, n1 = 0, n2 = 0;
     int n_img = 1;  // slice stacks in the call (work / out hold n_img stacks back to back)
     // bucketed atoms (build from atoms)
-    // (n_img * n_elems * n_pairs * n1 * ROW_SUB + 1) start offsets into items: bucket
-    // (image, element, pair, row, column mod ROW_SUB)
-    const unsigned* bucket_off = nullptr;
+    const unsigned* bucket_off = nullptr;  // (n_img * n_elems * n_pairs * n1 + 1) start offsets into items
     const unsigned* items = nullptr;       // (slice parity << 31) | column, grouped by bucket
     const int2* wq = nullptr;              // W_n2^m then i W_n2^m, m < n2, WQ_SCALE fixed point
     const int* img_slices = nullptr;       // per image slice count (<= n_slices); pairs beyond are skipped

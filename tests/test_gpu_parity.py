@@ -355,49 +355,6 @@ def test_build_slices_from_atoms_empty_and_outside(eng):
     np.testing.assert_array_equal(got, np.full_like(got, np.float32(1e-13)))
 
 
-@pytest.mark.parametrize("ns,n1,n2", [(12, 256, 256), (5, 128, 64), (3, 64, 256), (4, 512, 512)])
-def test_slice_sums_four_columns_equal_direct(eng, tmp_path, ns, n1, n2):
-    """Four columns per table lookup (atoms bucketed by column mod 4, an exact integer
-    DFT4 of the four partial sums) gives bitwise the slices of one lookup per atom and
-    column (EMSIM_GB300_SLICE_SUMS=direct, in a child process): square and rectangular
-    grids, and a row of 1200 atoms in one slice pair (64-bit sums)."""
-    import subprocess
-    import sys
-    rng = np.random.default_rng(n1 + 7 * n2 + ns)
-    zs = [6, 7, 8, 16]
-    mols = []
-    for k in range(2):
-        m = 3000 + 2000 * k
-        el = rng.choice(np.array(zs), size=m)
-        half = np.array([ns * 2.0 / 2 * 0.9, n1 * 0.5 / 2 * 0.9, n2 * 0.5 / 2 * 0.9])
-        xyz = ((rng.random((m, 3)) * 2 - 1) * half).astype(np.float32)
-        if k == 1:  # 1200 carbons in one row (x) of one slice (z), spread over the columns (y)
-            xyz[:1200, 0] = 0.3
-            xyz[:1200, 1] = 0.1
-            el[:1200] = 6
-        _, xyz_s, _, cnt = om.sort_elements_and_count(el, xyz, zs)
-        mols.append((xyz_s, cnt))
-    b = eng.MultiSlicesBuilder(zs, ns, n1, n2, 2.0, 0.5, 0.5)
-    assert b.atoms_path
-    got = _np(eng.build_slices_batch(b, mols))
-    np.savez(tmp_path / "mols.npz", *[a for mol in mols for a in mol])
-    code = ("import numpy as np, sys; sys.path.insert(0, %r)\n"
-            "from emsim_gb300 import backend\n"
-            "f = np.load(%r); a = [f['arr_%%d' %% i] for i in range(len(f.files))]\n"
-            "b = backend.MultiSlicesBuilder(%r, %d, %d, %d, 2.0, 0.5, 0.5)\n"
-            "out = backend.build_slices_batch(b, [(a[2 * i], a[2 * i + 1]) for i in range(len(a) // 2)])\n"
-            "np.save(%r, out.get())\n") % (
-        str(__import__("pathlib").Path(__file__).resolve().parent.parent), str(tmp_path / "mols.npz"), zs, ns, n1, n2,
-        str(tmp_path / "direct.npy"))
-    env = dict(__import__("os").environ, EMSIM_GB300_SLICE_SUMS="direct")
-    subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=300)
-    np.testing.assert_array_equal(got, np.load(tmp_path / "direct.npy"))
-    sf = om.scattering_factors_half(zs, n1, n2, 0.5, 0.5)
-    hist = om.bin_atoms_cuda(mols[1][0], mols[1][1], (ns, n1, n2), (2.0, 0.5, 0.5))
-    assert hist.max() >= 1  # the dense row is binned
-    assert om.rel_l2(got[1], om.make_slices(hist, sf, "fftw", np.float64)) < TOL
-
-
 def test_pipe_run_batch_device_front_end(eng):
     """run_batch (GPU centralisation, Z lookup, unsorted atoms) == reference-shaped path
     (host centralize + sort + bin + make) == oracle, for molecules of different element
