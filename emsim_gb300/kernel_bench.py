@@ -10,8 +10,9 @@ ncu captures of single kernels.
 
 cases: step (multislice_propagate), space (space_propagate), lens (lens_propagate),
 image (multislice_image: plane wave -> slices -> lens -> |psi|^2), slices
-(make_multi_slices), atoms (build_slices: slices straight from atoms, --atoms per image),
-bin (bin_atoms_multi_slices).
+(make_multi_slices), atoms (build_slices: slices straight from atoms, --atoms per image,
+uniform over the slab), blobs (build_slices of --batch seeded protein-like blobs of --atoms
+atoms in a 40 A sphere, as in the bench step), bin (bin_atoms_multi_slices).
 """
 from __future__ import annotations
 
@@ -44,7 +45,8 @@ def _time(fn, reps: int, flush: torch.Tensor) -> float:
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="step", choices=["step", "space", "lens", "image", "slices", "atoms", "bin"])
+    ap.add_argument("--case", default="step",
+                    choices=["step", "space", "lens", "image", "slices", "atoms", "blobs", "bin"])
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--slices", type=int, default=4)
@@ -115,6 +117,35 @@ def main(argv=None):
         t = _time(fn, args.reps, flush)
         out.update(elements=E, slices=S, seconds=t, slices_per_s=S / t,
                    algo_gbs=(4.0 * E + 4.0) * S * n * n / t / 1e9)
+    elif args.case == "blobs":
+        # the bench's workload: --batch seeded 50k-atom C/N/O/S blobs (40 A sphere), each
+        # centralised and sized as Pipe does (roi --n, pixel 1 A, 2 A slices)
+        from . import atoms as atm
+        from . import pot, synth
+        geo = []
+        for seed in range(B):
+            mol = atm.centralize(atm.AtomList(*synth.protein_blob(args.atoms, 40.0, seed)))
+            mol, uz, cnt = atm.sort_elements_and_count(mol)
+            ns, _, _ = pot.finalize_slice_size(tuple(mol.space), (1.0, 1.0), 2.0, (n, n), None)
+            geo.append((mol.coordinates, [int(z) for z in uz], cnt, ns))
+        if any(g[1] != geo[0][1] for g in geo):
+            raise SystemExit("blobs case: the seeded blobs need one element set")
+        S = max(g[3] for g in geo)
+        b = backend.MultiSlicesBuilder(geo[0][1], S, n, n, 2.0, 1.0, 1.0)
+        xyz = np.ascontiguousarray(np.concatenate([g[0] for g in geo]).astype(np.float32))
+        counts = np.stack([np.asarray(g[2]) for g in geo]).astype(np.uint32)
+        N = int(xyz.shape[0])
+        c = torch.from_numpy(xyz).to(dev)
+        cn = torch.from_numpy(counts.view(np.int32)).to(dev)
+        o = torch.empty((B, S, n, n), dtype=torch.float32, device=dev)
+        nbytes = int(_native.load().emsim_gb300_build_slices_workspace_size(b._plan.handle, N, B))
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        fn = lambda: _native.call("emsim_gb300_build_slices", b._plan.handle, P(c), N, P(cn), B, P(o), P(ws),  # noqa
+                                  nbytes, st())
+        for _ in range(args.warmup):
+            fn()
+        t = _time(fn, args.reps, flush)
+        out.update(batch=B, atoms=N, slices=S, seconds=t, images_per_s=B / t, slices_per_s=B * S / t)
     elif args.case == "atoms":
         zs = [6, 7, 8, 16]
         b = backend.MultiSlicesBuilder(zs, S, n, n, 2.0, 1.0, 1.0)
