@@ -227,3 +227,43 @@ def test_synthetic_blob_matches_oracle_generator():
     assert len(mix) == 4 and {r for _, _, r in mix} <= {256, 512}
     assert all(set(np.unique(el)) <= {1, 6, 7, 8, 16} for el, _, _ in mix)
     assert np.any(mix[1][0] == 1) and not np.any(mix[0][0] == 1)  # odd blobs carry ice
+
+
+def test_pending_images_reassemble_input_order():
+    """PendingImages (Pipe.submit_batch's handle) waits on its event once, returns the
+    images of its groups in input order as views of the page-locked buffers, and reports
+    done() from the event; a completed handle never waits.  Host logic, with a fake
+    event and CPU tensors standing in for the page-locked copies."""
+    import torch
+
+    from emsim_gb300.pipe import PendingImages
+
+    class FakeEvent:
+        def __init__(self):
+            self.waits = 0
+            self.ready = False
+
+        def query(self):
+            return self.ready
+
+        def synchronize(self):
+            self.waits += 1
+            self.ready = True
+
+    a = torch.arange(3 * 2 * 2, dtype=torch.float32).reshape(3, 2, 2)
+    b = 100 + torch.arange(2 * 4 * 4, dtype=torch.float32).reshape(2, 4, 4)
+    ev = FakeEvent()
+    p = PendingImages(5, [([4, 0, 2], a, None), ([1, 3], b, None)], ev)
+    assert not p.done()
+    out = p.result()
+    assert ev.waits == 1 and p.done()
+    assert [o.shape for o in out] == [(2, 2), (4, 4), (2, 2), (4, 4), (2, 2)]
+    np.testing.assert_array_equal(out[4], a[0].numpy())
+    np.testing.assert_array_equal(out[0], a[1].numpy())
+    np.testing.assert_array_equal(out[2], a[2].numpy())
+    np.testing.assert_array_equal(out[1], b[0].numpy())
+    np.testing.assert_array_equal(out[3], b[1].numpy())
+    assert np.shares_memory(out[0], a.numpy())  # views of the buffer, no copy
+    assert p.result() is out and ev.waits == 1
+    done = PendingImages.completed([np.zeros(2)])
+    assert done.done() and len(done.result()) == 1
