@@ -72,23 +72,6 @@ __host__ __device__ __forceinline__ float2 cmul_mi(float2 a) {
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// exp(i x) for the transmission phase x = sigma V.  x is reduced to r in about [-pi, pi]
-// by a two-constant Cody-Waite reduction (k = rint(x / 2 pi), r = x - k 2 pi with 2 pi
-// split into its nearest float and the float nearest to the rest, each product taken in
-// one fma), then the SFU sine and cosine of r (__sincosf: absolute error at most
-// 2^-21.41 on [-pi, pi], CUDA documentation).  A few instructions against the tens of the
-// full-range sincosf; the error stays below 1e-6 for |x| up to 10^4 (tested against FP64).
-__device__ __forceinline__ float2 phase_exp(float x) {
-    constexpr float INV_2PI = 0.159154943091895335769f;
-    constexpr float TWO_PI_HI = 6.28318548202514648438f;   // float nearest to 2 pi
-    constexpr float TWO_PI_LO = -1.74845560007449705e-07f;  // 2 pi - TWO_PI_HI
-    const float k = rintf(x * INV_2PI);
-    const float r = fmaf(-k, TWO_PI_LO, fmaf(-k, TWO_PI_HI, x));
-    float s, c;
-    __sincosf(r, &s, &c);
-    return make_float2(c, s);
-}
-
 // fftfreq integer of FFT index i for length n (i for i < ceil(n/2), else i - n);
 // the reference reaches the same integer through its ifftshift index arithmetic
 // (WavePropagator_kernel.cu:73-78).

@@ -317,7 +317,9 @@ __global__ void transmit_kernel(const float2* in, const float* __restrict__ slic
                                 float sigma, long long in_stride, long long slice_stride, long long out_stride) {
     const long long img = blockIdx.y;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        out[img * out_stride + i] = cmul(in[img * in_stride + i], phase_exp(sigma * slice[img * slice_stride + i]));
+        float s, c;
+        sincosf(sigma * slice[img * slice_stride + i], &s, &c);
+        out[img * out_stride + i] = cmul(in[img * in_stride + i], make_float2(c, s));
     }
 }
 

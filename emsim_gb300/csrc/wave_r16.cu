@@ -82,7 +82,11 @@ __global__ void __launch_bounds__(THREADS, 2) row16_kernel(RowArgs a, int B, int
         if (OPS & ROW_IFFT) fft16::fft256<true, true>(v, stage, b, t, fft16::RowSlot{}, a.tw);
         if (OPS & ROW_TRANSMIT) {
 #pragma unroll
-            for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], phase_exp(a.sigma * vs[m]));
+            for (int m = 0; m < 16; ++m) {
+                float s, c;
+                sincosf(a.sigma * vs[m], &s, &c);
+                v[m] = cmul(v[m], make_float2(c, s));
+            }
         }
         if (OPS & ROW_FFT) fft16::fft256<false, true>(v, stage, b, t, fft16::RowSlot{}, a.tw);
 

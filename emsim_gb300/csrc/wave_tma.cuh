@@ -112,7 +112,11 @@ __global__ void __launch_bounds__(RowTma<N>::THREADS, RowTma<N>::MIN_BLOCKS)
         }
         if (OPS & ROW_TRANSMIT) {
 #pragma unroll
-            for (int m = 0; m < 8; ++m) v[m] = cmul(v[m], phase_exp(a.sigma * vs[m]));
+            for (int m = 0; m < 8; ++m) {
+                float s, c;
+                sincosf(a.sigma * vs[m], &s, &c);
+                v[m] = cmul(v[m], make_float2(c, s));
+            }
         }
         if (OPS & ROW_STORE_PHI) {
             float2* ph = a.phi + img * a.phi_img_stride + row * N;

@@ -73,25 +73,6 @@ def test_init_wave_and_intensity_exact(eng):
     np.testing.assert_array_equal(got, (x.real * x.real + x.imag * x.imag).astype(np.float32))
 
 
-def test_transmission_phase_error_bound(eng):
-    """exp(i sigma V) of the transmit (a Cody-Waite reduction to [-pi, pi], then the SFU
-    sine and cosine) against FP64 exp(i x) of the same float32 phase x = fl(sigma V):
-    absolute error <= 1e-6 for phases of 0 to 10^4 rad, both signs (the SFU bound is
-    2^-21.41 on [-pi, pi]); |exp(i x)| = 1 to 1e-6."""
-    n, kev = 128, 200.0
-    rng = np.random.default_rng(77)
-    sig32 = np.float32(om.wave_length(kev) * om.relativity_gamma(kev))
-    phase = np.concatenate([rng.uniform(-np.pi, np.pi, n * n // 4), rng.uniform(-60, 60, n * n // 4),
-                            rng.uniform(-1e4, 1e4, n * n // 4), np.linspace(-40, 40, n * n // 4)])
-    v = (phase / np.float64(sig32)).astype(np.float32).reshape(n, n)
-    x = (sig32 * v).astype(np.float64)  # the float32 product the kernel forms
-    wp = eng.WavePropagator(n, n, 0.5, 0.5, kev)
-    got = _np(wp.slice_transmit(np.ones((n, n), np.complex64), v)).astype(np.complex128)
-    err = np.abs(got - np.exp(1j * x))
-    assert err.max() <= 1e-6, err.max()
-    assert np.abs(np.abs(got) - 1).max() <= 1e-6
-
-
 def test_multislice_edge_cases(eng):
     rng = np.random.default_rng(11)
     wp = eng.WavePropagator(64, 64, 0.5, 0.5, 200.0)
