@@ -125,17 +125,15 @@ struct ColThreads {
     static constexpr int MIN_BLOCKS = (N / 8 >= 256) ? 1 : 2;
 };
 
-// x P(k1, k2) / N inside the band-limit disc, 0 outside, for column `col`, rows t + m*T;
-// p1s: the row factors staged in shared memory (nullptr: read a.p1)
+// x P(k1, k2) / N inside the band-limit disc, 0 outside, for column `col`, rows t + m*T
 template <int N>
-__device__ __forceinline__ void propagate_col(float2 (&v)[8], int col, int t, const ColArgs& a,
-                                              const float4* p1s = nullptr) {
+__device__ __forceinline__ void propagate_col(float2 (&v)[8], int col, int t, const ColArgs& a) {
     constexpr int T = N / 8;
     const int k2a = abs(fftfreq_int(col, a.n_cols));
     const float2 p2 = __ldg(a.p2 + col);
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
-        const float4 q = p1s ? p1s[t + m * T] : __ldg(a.p1 + t + m * T);
+        const float4 q = __ldg(a.p1 + t + m * T);
         v[m] = (k2a <= __float_as_int(q.z)) ? cmul(v[m], cmul(make_float2(q.x, q.y), p2)) : make_float2(0.f, 0.f);
     }
 }

@@ -178,8 +178,6 @@ __global__ void __launch_bounds__(512, 2)
     float2* stage0 = reinterpret_cast<float2*>(smem_raw);
     float2* stage1 = stage0 + te;
     uint64_t* bar = reinterpret_cast<uint64_t*>(stage1 + te);
-    // the propagator's row factors, read once per CTA instead of once per tile
-    float4* s_p1 = reinterpret_cast<float4*>(bar + 2);
     const ColSwz addr{B, B >= 16 ? 0 : (16 / B) - 1};
     const int live_per_img = lt_lo + lt_hi;
     const int n_tiles = live_per_img * n_img;
@@ -206,8 +204,6 @@ __global__ void __launch_bounds__(512, 2)
         tma::mbar_init(&bar[1], 1);
         tma::fence_mbar_init();
     }
-    if (MODE == COL_PROPAGATE)
-        for (int i = tid; i < N; i += blockDim.x) s_p1[i] = __ldg(a.p1 + i);
     __syncthreads();
     if (tid == 0) {
         if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
@@ -233,7 +229,7 @@ __global__ void __launch_bounds__(512, 2)
         const int col = ct * B + b;
         if (MODE != COL_INV) fft::fft_regs<N, false, false>(v, stage, b, t, addr, a.tw);
         if (MODE == COL_PROPAGATE) {
-            propagate_col<N>(v, col, t, a, s_p1);
+            propagate_col<N>(v, col, t, a);
         } else if (MODE == COL_LENS) {
             const int k2 = fftfreq_int(col, a.n_cols);
             const double fy = (double)k2 * a.dfy64;
@@ -325,7 +321,7 @@ int launch_col_tma_n(int mode, const ColArgs& a, int n_img, cudaStream_t st) {
     const int threads = B * T;
     const int tiles_per_img = a.n_cols / B;
     const LiveTiles lt = mode == COL_PROPAGATE ? live_tiles(a, B, tiles_per_img) : LiveTiles{tiles_per_img, 0};
-    const size_t smem = 2 * (size_t)N * B * sizeof(float2) + 2 * sizeof(uint64_t) + (size_t)N * sizeof(float4);
+    const size_t smem = 2 * (size_t)N * B * sizeof(float2) + 2 * sizeof(uint64_t);
     CUtensorMap map;
     EMSIM_TRY(make_col_tensor_map(&map, a.data, (long long)n_img * N, a.n_cols, B, ColTma<N>::BOXR));
     switch (mode) {
