@@ -267,3 +267,57 @@ def test_pending_images_reassemble_input_order():
     assert p.result() is out and ev.waits == 1
     done = PendingImages.completed([np.zeros(2)])
     assert done.done() and len(done.result()) == 1
+
+
+def test_emsim_results_in_input_order_one_at_a_time_and_batched():
+    """EMSim (emsim/simulator.py:21-91) hands every image to the handler in input order
+    with its label, logs and skips a failing molecule; with batch_size > 1 it submits
+    groups through submit_batch, two in flight, and a group that fails as a whole (at
+    submission or when collected) is rerun molecule by molecule.  A fake pipe stands in
+    for the GPU."""
+    from emsim_gb300.simulator import EMSim
+
+    class Mol:
+        def __init__(self, k, bad=False, late=False):
+            self.label, self.k, self.bad, self.late = f"m{k}", k, bad, late
+
+    class FakePending:
+        def __init__(self, imgs, fail):
+            self.imgs, self.fail = imgs, fail
+
+        def result(self):
+            if self.fail:
+                raise RuntimeError("device error reported at collection")
+            return self.imgs
+
+    class FakePipe:
+        def __init__(self):
+            self.groups, self.single = [], []
+
+        def run(self, mol):
+            self.single.append(mol.k)
+            if mol.bad:
+                raise ValueError("bad molecule")
+            return np.full(3, mol.k, np.float32)
+
+        def submit_batch(self, mols):
+            self.groups.append([m.k for m in mols])
+            if any(m.bad for m in mols):
+                raise ValueError("a bad molecule in the group")
+            return FakePending([np.full(3, m.k, np.float32) for m in mols], any(m.late for m in mols))
+
+    mols = [Mol(k, bad=(k == 5), late=(k == 9)) for k in range(11)]
+    want = [f"m{k}" for k in range(11) if k != 5]
+    for bs in (1, 4):
+        got = []
+        fake = FakePipe()
+        EMSim(fake, mols, lambda img, label: got.append((label, img.copy())), batch_size=bs).run()
+        assert [lab for lab, _ in got] == want
+        assert all(img[0] == int(lab[1:]) for lab, img in got)
+        if bs == 1:
+            assert fake.groups == [] and fake.single == list(range(11))
+        else:
+            assert fake.groups == [[0, 1, 2, 3], [4, 5, 6, 7], [8, 9, 10]]
+            assert fake.single == [4, 5, 6, 7, 8, 9, 10]  # the two failed groups, rerun one by one
+    with pytest.raises(ValueError):
+        EMSim(FakePipe(), mols, lambda *a: None, batch_size=0)
