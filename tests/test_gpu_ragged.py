@@ -147,3 +147,21 @@ def test_submitted_batches_in_flight_equal_serial(eng):
         for a, b in zip(g, s):
             assert isinstance(a, np.ndarray)
             np.testing.assert_array_equal(a, b)
+
+
+def test_emsim_batched_equals_run_batch(eng):
+    """simulator.EMSim with batch_size 2 (groups through Pipe.submit_batch, two in
+    flight) hands each molecule's image to the handler, bitwise equal to run_batch."""
+    torch, atoms, backend, pipe, tem = eng
+    from emsim_gb300.simulator import EMSim
+    rng = np.random.default_rng(21)
+    specs = [(1200, 8.0, 14.0), (900, 6.0, 14.0), (1500, 10.0, 14.0), (700, 5.0, 14.0), (1100, 7.0, 14.0)]
+    mols = [atoms.AtomList(el, xyz, label=f"mol{i}") for i, (el, xyz) in enumerate(_mols(rng, specs))]
+    m = tem.TEM(electron_dose=20, beam_energy_kev=200, cs_mm=1.3, defocus=700, aperture=10e-3)
+    p = pipe.Pipe(m, resolution=2.0, slice_thickness=2.0, roi=64, add_water=False)
+    ref = p.run_batch(mols, to_host=True)
+    got = {}
+    EMSim(p, mols, lambda img, label: got.__setitem__(label, np.array(img)), batch_size=2).run()
+    assert sorted(got) == [f"mol{i}" for i in range(len(mols))]
+    for i in range(len(mols)):
+        np.testing.assert_array_equal(got[f"mol{i}"], ref[i])
