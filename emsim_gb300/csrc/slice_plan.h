@@ -14,7 +14,7 @@ struct emsim_gb300_slice_plan {
     float2* tw1 = nullptr;  // generic path twiddles exp(-2 pi i m / n)
     float2* tw2 = nullptr;
     float* filt = nullptr;  // (n_elems, n1, n2): F(k) * SF_e(k) / N
-    int2* wq = nullptr;     // fast path: W_n2^m = exp(-2 pi i m / n2) as 2^30-scaled fixed point
+    int2* wq = nullptr;     // fast path: W_n2^m then i W_n2^m, m < n2, 2^22-scaled fixed point (WQ_SCALE)
 };
 
 namespace emsim_gb300 {
