@@ -22,6 +22,10 @@ SIGNATURES = {
     "emsim_gb300_abi_version": (_c_int, []),
     "emsim_gb300_last_error": (ctypes.c_char_p, []),
     "emsim_gb300_check_device_error": (_c_int, [ctypes.POINTER(ctypes.c_int)]),
+    "emsim_gb300_peek_device_error": (_c_int, [ctypes.POINTER(ctypes.c_int)]),
+    "emsim_gb300_set_wait_limit_ns": (_c_int, [ctypes.c_ulonglong]),
+    "emsim_gb300_get_wait_limit_ns": (ctypes.c_ulonglong, []),
+    "emsim_gb300_wait_timeout_probe": (_c_int, [ctypes.c_ulonglong, _c_vp, _c_vp]),
     "emsim_gb300_wave_plan_create": (_c_int, [_c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _pp]),
     "emsim_gb300_wave_plan_destroy": (_c_int, [_c_vp]),
     "emsim_gb300_init_wave": (_c_int, [_c_vp, _c_dbl, _c_vp, _c_int, _c_vp]),
@@ -128,6 +132,29 @@ def call(name: str, *args) -> None:
 
 def last_error() -> str:
     return load().emsim_gb300_last_error().decode(errors="replace")
+
+
+class DeviceWaitTimeout(RuntimeError):
+    """A pipelined kernel's bounded wait for a tile copy gave up; the results of the work
+    queued before this was noticed are invalid.  The device error word stays set until
+    :func:`check_device_error` reads and clears it."""
+
+
+def peek_device_error() -> int:
+    """The current device's error word, read without synchronising or clearing it (kernels
+    that have not finished yet are not reflected)."""
+    code = ctypes.c_int(0)
+    call("emsim_gb300_peek_device_error", ctypes.byref(code))
+    return int(code.value)
+
+
+def raise_on_device_error() -> None:
+    """Raise :class:`DeviceWaitTimeout` when the current device's error word is set.  Call
+    it after the host has waited for the work it wants to vouch for."""
+    code = peek_device_error()
+    if code != 0:
+        raise DeviceWaitTimeout(f"device error word = {code}: a kernel's bounded wait for a tile copy timed out; "
+                                f"results computed since the last emsim_gb300_check_device_error are invalid")
 
 
 def check_device_error() -> int:

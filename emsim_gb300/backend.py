@@ -35,7 +35,13 @@ class DeviceArray(torch.Tensor):
     """A torch CUDA tensor with ``get()`` returning a numpy copy (cupy's spelling)."""
 
     def get(self) -> np.ndarray:
-        return self.detach().cpu().numpy()
+        """Host copy; raises ``DeviceWaitTimeout`` when a kernel of the device gave up a
+        bounded wait (its results would be invalid)."""
+        out = self.detach().cpu().numpy()
+        if self.is_cuda:
+            with torch.cuda.device(self.device):
+                _native.raise_on_device_error()
+        return out
 
 
 def _wrap(t: torch.Tensor) -> DeviceArray:

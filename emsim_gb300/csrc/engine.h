@@ -10,6 +10,10 @@
 
 namespace emsim_gb300 {
 
+// Limit of the pipelined kernels' bounded mbarrier waits (ns), process-wide
+// (emsim_gb300_set_wait_limit_ns); every RowArgs / ColArgs takes it when constructed.
+unsigned long long wait_limit_ns();
+
 // ---------------------------------------------------------------------------
 // row passes: one CTA holds B whole rows; each row is transformed in registers/smem
 // ---------------------------------------------------------------------------
@@ -42,6 +46,7 @@ struct RowArgs {
     int n_rows = 0;
     const float2* tw = nullptr;  // per-pass twiddle tables of the device (twiddle_table())
     int* err = nullptr;          // device error word (error_word())
+    unsigned long long wait_ns = wait_limit_ns();  // bounded mbarrier wait limit
 };
 
 // ---------------------------------------------------------------------------
@@ -57,6 +62,7 @@ enum ColMode : int {
 struct ColArgs {
     const float2* tw = nullptr;  // per-pass twiddle tables of the device (twiddle_table())
     int* err = nullptr;          // device error word (error_word())
+    unsigned long long wait_ns = wait_limit_ns();  // bounded mbarrier wait limit
     float2* data = nullptr;
     long long img_stride = 0;
     int n_rows = 0;  // FFT length along columns (n1)

@@ -20,10 +20,15 @@
 //    reads), but two calls that overlap on the GPU (unordered streams) race on it;
 //  * the buffer's device address is looked up once per device, by the first call made
 //    with that device current (cudaGetSymbolAddress); make that first call before any
-//    stream capture.
+//    stream capture.  A call whose plan belongs to another device is refused before that
+//    look-up, so it reserves nothing on the wrong device;
+//  * the looked-up address, like every plan, belongs to the device's context:
+//    cudaDeviceReset invalidates it, and the entry point must not be called on a device
+//    after that device was reset.
 #include <mutex>
 
 #include "common.cuh"
+#include "slice_plan.h"
 
 // The name is a host-side stand-in in host code: kernels only ever receive the device
 // address that cudaGetSymbolAddress returns for it.
@@ -42,6 +47,7 @@ extern "C" int emsim_gb300_make_slices_noalloc(emsim_gb300_slice_plan* plan, con
     using emsim_gb300::set_error;
     EMSIM_REQUIRE(plan != nullptr && hist != nullptr && out != nullptr, EMSIM_GB300_ERR_INVALID,
                   "make_slices_noalloc: null plan, histogram or output");
+    EMSIM_TRY(emsim_gb300::check_slice_device(plan));
     const size_t need = emsim_gb300_make_slices_workspace_size(plan);
     if (need > (size_t)EMSIM_GB300_NOALLOC_SCRATCH_BYTES) {
         set_error("make_slices_noalloc: this plan needs " + std::to_string(need) +

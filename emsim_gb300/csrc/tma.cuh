@@ -12,8 +12,20 @@ namespace tma {
 // device error word written by kernels whose barrier waits time out (see check_error)
 enum DeviceError : int { DEV_OK = 0, DEV_MBAR_TIMEOUT = 1 };
 
-// an mbarrier wait gives up after this much global time (ns)
-constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;
+// default limit of a bounded mbarrier wait (ns of global time); kernels get the limit in
+// their arguments (RowArgs / ColArgs::wait_ns, emsim_gb300_set_wait_limit_ns)
+constexpr unsigned long long DEFAULT_WAIT_LIMIT_NS = 2000000000ull;
+// the shortest limit the C ABI accepts for the pipelined kernels
+constexpr unsigned long long MIN_WAIT_LIMIT_NS = 1000000ull;
+
+// Record a device error code in the error word (mapped page-locked host memory, one word
+// per device: the host reads it without synchronising the device).
+__device__ __forceinline__ void record_error(int* err, int code) {
+    if (err) {
+        *reinterpret_cast<volatile int*>(err) = code;
+        __threadfence_system();
+    }
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -67,25 +79,34 @@ __device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t pa
 }
 
 // Wait for the phase with the given parity, suspending between polls; false after
-// WAIT_LIMIT_NS without completion.
-__device__ __forceinline__ bool mbar_wait_suspend(uint64_t* bar, uint32_t parity) {
+// limit_ns of global time without completion.
+__device__ __forceinline__ bool mbar_wait_suspend(uint64_t* bar, uint32_t parity,
+                                                  unsigned long long limit_ns = DEFAULT_WAIT_LIMIT_NS) {
     const uint64_t t0 = global_ns();
     for (;;) {
         if (mbar_try_wait_suspend(bar, parity, 100000u)) return true;
-        if (global_ns() - t0 > WAIT_LIMIT_NS) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
 }
 
-// Wait for the phase with the given parity; false after WAIT_LIMIT_NS without completion.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Wait for the phase with the given parity; false after limit_ns of global time without
+// completion.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          unsigned long long limit_ns = DEFAULT_WAIT_LIMIT_NS) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
 #pragma unroll 1
         for (int i = 0; i < 64; ++i)
             if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > WAIT_LIMIT_NS) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
+}
+
+// After a wait gave up: wait for a copy of this CTA that is still in flight with at least
+// the default limit, so that it lands before the CTA's shared memory is released.
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
+    mbar_wait(bar, parity, limit_ns > DEFAULT_WAIT_LIMIT_NS ? limit_ns : DEFAULT_WAIT_LIMIT_NS);
 }
 
 // contiguous global -> shared copy of `bytes` (multiple of 16, both addresses 16-byte

@@ -155,7 +155,7 @@ __device__ __forceinline__ void twiddle_scatter(DftSmem& s, int m, const float (
 
 // one 16-point stage on the A tile: 6 MMAs (hi.hi, hi.lo, lo.hi over 2 K steps), then
 // every thread reads its D row; false when the completion wait timed out
-__device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB]) {
+__device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB], unsigned long long wait_ns) {
     tma::fence_proxy_async();
     umma::fence_before_sync();
     __syncthreads();
@@ -178,7 +178,7 @@ __device__ __forceinline__ bool stage(DftSmem& s, uint32_t& phase, float (&d)[KB
     }
     // the first WAIT_WARPS warps wait for the completion (suspended, not spinning); the
     // others wait at the barrier
-    const bool ok = threadIdx.x >= 32 * WAIT_WARPS || tma::mbar_wait_suspend(&s.bar, phase);
+    const bool ok = threadIdx.x >= 32 * WAIT_WARPS || tma::mbar_wait_suspend(&s.bar, phase, wait_ns);
     phase ^= 1u;
     if (__syncthreads_or(!ok)) return false;
     umma::fence_after_sync();
@@ -213,8 +213,8 @@ __device__ void setup(DftSmem& s, const float2* tw4096, const float4* p1 = nullp
 
 // ok == false: a completion wait gave up; wait once more (bounded) for the MMAs in
 // flight before the tensor memory is freed
-__device__ void teardown(DftSmem& s, bool ok, uint32_t phase) {
-    if (!ok) tma::mbar_wait(&s.bar, phase ^ 1u);
+__device__ void teardown(DftSmem& s, bool ok, uint32_t phase, unsigned long long wait_ns) {
+    if (!ok) tma::mbar_drain(&s.bar, phase ^ 1u, wait_ns);
     umma::fence_before_sync();
     __syncthreads();
     if (threadIdx.x < 32) umma::tmem_dealloc(s.tmem, TMEM_COLS);
@@ -246,9 +246,9 @@ __global__ void __launch_bounds__(THREADS, 6) row_bf16_kernel(RowArgs a, int n_t
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) pot[k1] = __ldg(vsrc + lo4 + NS * k1);  // used after the inverse
         write_row<true>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
         twiddle_scatter<true>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
         // thread (r, k2) holds conj(psi[k2 + 16 k1]): transmit, then it is the forward
         // transform's stage-A row (r, n1) with n1 = k2, n2 = k1
 #pragma unroll
@@ -260,15 +260,15 @@ __global__ void __launch_bounds__(THREADS, 6) row_bf16_kernel(RowArgs a, int n_t
             d[2 * k1 + 1] = t.y;
         }
         write_row<false>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
         twiddle_scatter<true>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
         float2* dst = a.out + img * a.out_img_stride + (long long)row * N;
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) dst[lo4 + NS * k1] = make_float2(d[2 * k1], d[2 * k1 + 1]);
     }
-    if (!ok && m == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
-    teardown(s, ok, phase);
+    if (!ok && m == 0) tma::record_error(a.err, tma::DEV_MBAR_TIMEOUT);
+    teardown(s, ok, phase, a.wait_ns);
 }
 
 // ---- column pass: forward column FFT, x P(k) inside the band-limit / N, inverse --------
@@ -298,9 +298,9 @@ __global__ void __launch_bounds__(THREADS, 6) col_bf16_kernel(ColArgs a, int til
             d[2 * n2 + 1] = v.y;
         }
         write_row<false>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
         twiddle_scatter<false>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
         {
             // thread (c, k2) holds X[k] at k = k2 + 16 k1 of its column
             const int k2a = abs(fftfreq_int(col, a.n_cols));
@@ -316,9 +316,9 @@ __global__ void __launch_bounds__(THREADS, 6) col_bf16_kernel(ColArgs a, int til
             }
         }
         write_row<true>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
         twiddle_scatter<false>(s, m, d);
-        if (!(ok = stage(s, phase, d))) break;
+        if (!(ok = stage(s, phase, d, a.wait_ns))) break;
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) base[(hi3 + NS * k1) * ld] = make_float2(d[2 * k1], -d[2 * k1 + 1]);
     }
@@ -331,9 +331,9 @@ __global__ void __launch_bounds__(THREADS, 6) col_bf16_kernel(ColArgs a, int til
             for (int q = 0; q < N / 16; ++q) base[(hi3 + 16 * q) * ld] = make_float2(0.f, 0.f);
         }
     } else if (m == 0) {
-        atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
+        tma::record_error(a.err, tma::DEV_MBAR_TIMEOUT);
     }
-    teardown(s, ok, phase);
+    teardown(s, ok, phase, a.wait_ns);
 }
 
 constexpr size_t ROW_SMEM = sizeof(DftSmem);

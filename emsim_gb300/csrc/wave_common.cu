@@ -1,5 +1,6 @@
 // Size dispatch of the fused passes, the twiddle table, the generic (any-size) path and
 // the element-wise kernels of the wave propagator.
+#include <atomic>
 #include <mutex>
 #include <set>
 #include <utility>
@@ -17,8 +18,14 @@ namespace emsim_gb300 {
 
 // exp(-2 pi i m / TW_SIZE); one copy per device, written once by init_twiddle_kernel
 static __device__ float2 g_twiddle[fft::TW_SIZE];
-// error word: kernels record tma::DEV_MBAR_TIMEOUT here when a bounded wait gives up
-static __device__ int g_dev_error;
+// error words: kernels record tma::DEV_MBAR_TIMEOUT in their device's word when a bounded
+// wait gives up.  One int per device in mapped page-locked host memory, so that the host
+// can read a word without synchronising the device (emsim_gb300_peek_device_error).
+static int* g_err_host = nullptr;
+
+// limit of the pipelined kernels' bounded waits (ns)
+static std::atomic<unsigned long long> g_wait_limit_ns{tma::DEFAULT_WAIT_LIMIT_NS};
+unsigned long long wait_limit_ns() { return g_wait_limit_ns.load(std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------------
 // error string (per host thread)
@@ -57,8 +64,13 @@ int ensure_twiddles(int device) {
     void* addr = nullptr;
     EMSIM_CHECK_CUDA(cudaGetSymbolAddress(&addr, g_twiddle));
     g_twiddle_addr[device] = (const float2*)addr;
+    if (!g_err_host) {
+        EMSIM_CHECK_CUDA(cudaHostAlloc((void**)&g_err_host, 64 * sizeof(int),
+                                       cudaHostAllocMapped | cudaHostAllocPortable));
+        std::memset(g_err_host, 0, 64 * sizeof(int));
+    }
     void* eaddr = nullptr;
-    EMSIM_CHECK_CUDA(cudaGetSymbolAddress(&eaddr, g_dev_error));
+    EMSIM_CHECK_CUDA(cudaHostGetDevicePointer(&eaddr, g_err_host + device, 0));
     g_error_addr[device] = (int*)eaddr;
     g_twiddle_ready.insert(device);
     return EMSIM_GB300_OK;
@@ -459,9 +471,65 @@ extern "C" int emsim_gb300_check_device_error(int* code) {
     EMSIM_CHECK_CUDA(cudaGetDevice(&dev));
     EMSIM_TRY(ensure_twiddles(dev));
     EMSIM_CHECK_CUDA(cudaDeviceSynchronize());
-    int zero = 0;
-    EMSIM_CHECK_CUDA(cudaMemcpyFromSymbol(code, g_dev_error, sizeof(int)));
-    EMSIM_CHECK_CUDA(cudaMemcpyToSymbol(g_dev_error, &zero, sizeof(int)));
+    volatile int* w = g_err_host + dev;
+    *code = *w;
+    *w = 0;
+    return EMSIM_GB300_OK;
+}
+
+extern "C" int emsim_gb300_peek_device_error(int* code) {
+    using namespace emsim_gb300;
+    EMSIM_REQUIRE(code != nullptr, EMSIM_GB300_ERR_INVALID, "peek_device_error: null output");
+    *code = 0;
+    if (!g_err_host) return EMSIM_GB300_OK;  // no kernel of this library has run yet
+    int dev = 0;
+    EMSIM_CHECK_CUDA(cudaGetDevice(&dev));
+    EMSIM_REQUIRE(dev >= 0 && dev < 64, EMSIM_GB300_ERR_UNSUPPORTED, "device index above 63");
+    *code = *(volatile int*)(g_err_host + dev);
+    return EMSIM_GB300_OK;
+}
+
+extern "C" int emsim_gb300_set_wait_limit_ns(unsigned long long ns) {
+    using namespace emsim_gb300;
+    EMSIM_REQUIRE(ns >= tma::MIN_WAIT_LIMIT_NS, EMSIM_GB300_ERR_INVALID,
+                  "set_wait_limit_ns: the limit must be at least 1 ms (1000000 ns)");
+    g_wait_limit_ns.store(ns, std::memory_order_relaxed);
+    return EMSIM_GB300_OK;
+}
+
+extern "C" unsigned long long emsim_gb300_get_wait_limit_ns(void) { return emsim_gb300::wait_limit_ns(); }
+
+namespace emsim_gb300 {
+// One CTA waits on an mbarrier that nothing arrives at (no copy is issued, so nothing is
+// in flight): the bounded wait gives up after limit_ns and the kernel records
+// DEV_MBAR_TIMEOUT in the error word, exactly as a pipelined pass does when a tile copy
+// never lands.
+__global__ void wait_timeout_probe_kernel(int* err, unsigned long long limit_ns, int* result) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        tma::mbar_init(&bar, 1);
+        tma::fence_mbar_init();
+    }
+    __syncthreads();
+    const bool ok = tma::mbar_wait(&bar, 0, limit_ns);
+    if (threadIdx.x == 0) {
+        if (!ok) tma::record_error(err, tma::DEV_MBAR_TIMEOUT);
+        *result = ok ? 1 : 0;
+    }
+}
+}  // namespace emsim_gb300
+
+extern "C" int emsim_gb300_wait_timeout_probe(unsigned long long limit_ns, int* completed, void* stream) {
+    using namespace emsim_gb300;
+    EMSIM_REQUIRE(completed != nullptr, EMSIM_GB300_ERR_INVALID, "wait_timeout_probe: null output");
+    EMSIM_REQUIRE(limit_ns >= 1000ull && limit_ns <= tma::DEFAULT_WAIT_LIMIT_NS, EMSIM_GB300_ERR_INVALID,
+                  "wait_timeout_probe: limit must be in [1 us, 2 s]");
+    int dev = 0;
+    EMSIM_CHECK_CUDA(cudaGetDevice(&dev));
+    EMSIM_TRY(ensure_twiddles(dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    wait_timeout_probe_kernel<<<1, 32, 0, st>>>(error_word(), limit_ns, completed);
+    EMSIM_CHECK_LAUNCH();
     return EMSIM_GB300_OK;
 }
 extern "C" int emsim_gb300_abi_version(void) { return EMSIM_GB300_ABI_VERSION; }

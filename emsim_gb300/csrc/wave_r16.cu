@@ -57,9 +57,9 @@ __global__ void __launch_bounds__(THREADS, 2) row16_kernel(RowArgs a, int B, int
     for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++it) {
         const int buf = it & 1;
         float2* stage = buf ? stage1 : stage0;
-        if (pipelined && !tma::mbar_wait(&bar[buf], (it >> 1) & 1)) {
-            if (tid == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
-            tma::mbar_wait(&bar[buf ^ 1], ((it + 1) >> 1) & 1);
+        if (pipelined && !tma::mbar_wait(&bar[buf], (it >> 1) & 1, a.wait_ns)) {
+            if (tid == 0) tma::record_error(a.err, tma::DEV_MBAR_TIMEOUT);
+            tma::mbar_drain(&bar[buf ^ 1], ((it + 1) >> 1) & 1, a.wait_ns);
             return;
         }
         float2 v[16];
@@ -210,9 +210,9 @@ __global__ void __launch_bounds__(COL_THREADS, 1)
     for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++it) {
         const int buf = it & 1;
         float2* stage = buf ? stage1 : stage0;
-        if (!tma::mbar_wait(&bar[buf], (it >> 1) & 1)) {
-            if (tid == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
-            tma::mbar_wait(&bar[buf ^ 1], ((it + 1) >> 1) & 1);
+        if (!tma::mbar_wait(&bar[buf], (it >> 1) & 1, a.wait_ns)) {
+            if (tid == 0) tma::record_error(a.err, tma::DEV_MBAR_TIMEOUT);
+            tma::mbar_drain(&bar[buf ^ 1], ((it + 1) >> 1) & 1, a.wait_ns);
             return;
         }
         float2 v[16];

@@ -9,9 +9,9 @@
 // CTA needs just two tiles of shared memory.  Results go straight from registers to
 // global memory with coalesced stores.
 //
-// Every barrier wait is bounded (tma::WAIT_LIMIT_NS); on timeout the kernel records
-// tma::DEV_MBAR_TIMEOUT in the device error word, gives its own in-flight copies a
-// bounded chance to land, and returns.
+// Every barrier wait is bounded (the wait_ns of the kernel's arguments); on timeout the
+// kernel records tma::DEV_MBAR_TIMEOUT in the device error word, waits (bounded, at least
+// the default limit) for its own copy still in flight, and returns.
 #pragma once
 
 #include "tma.cuh"
@@ -74,9 +74,9 @@ __global__ void __launch_bounds__(RowTma<N>::THREADS, RowTma<N>::MIN_BLOCKS)
     for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++it) {
         const int buf = it & 1;
         float2* stage = buf ? stage1 : stage0;
-        if (pipelined && !tma::mbar_wait(&bar[buf], (it >> 1) & 1)) {
-            if (tid == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
-            tma::mbar_wait(&bar[buf ^ 1], ((it + 1) >> 1) & 1);
+        if (pipelined && !tma::mbar_wait(&bar[buf], (it >> 1) & 1, a.wait_ns)) {
+            if (tid == 0) tma::record_error(a.err, tma::DEV_MBAR_TIMEOUT);
+            tma::mbar_drain(&bar[buf ^ 1], ((it + 1) >> 1) & 1, a.wait_ns);
             return;
         }
         float2 v[8];
@@ -214,9 +214,9 @@ __global__ void __launch_bounds__(512, 2)
     for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++it) {
         const int buf = it & 1;
         float2* stage = buf ? stage1 : stage0;
-        if (!tma::mbar_wait(&bar[buf], (it >> 1) & 1)) {
-            if (tid == 0) atomicExch(a.err, tma::DEV_MBAR_TIMEOUT);
-            tma::mbar_wait(&bar[buf ^ 1], ((it + 1) >> 1) & 1);
+        if (!tma::mbar_wait(&bar[buf], (it >> 1) & 1, a.wait_ns)) {
+            if (tid == 0) tma::record_error(a.err, tma::DEV_MBAR_TIMEOUT);
+            tma::mbar_drain(&bar[buf ^ 1], ((it + 1) >> 1) & 1, a.wait_ns);
             return;
         }
         float2 v[8];

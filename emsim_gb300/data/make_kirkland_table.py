@@ -8,18 +8,17 @@ The engine needs exactly the same numbers, so this script re-expresses that tabl
 a plain CSV (one row per Z: a1..a3, b1..b3, c1..c3, d1..d3), rounded to float32 the
 way ``emsim/elem.py:309`` rounds it.
 
-Usage:  python emsim_gb300/data/make_kirkland_table.py [path/to/atom_params.txt]
+Usage:  python emsim_gb300/data/make_kirkland_table.py path/to/emsim/assets/atom_params.txt
 """
 import sys
 from pathlib import Path
 
 import numpy as np
 
-DEFAULT_SRC = Path("/root/reference/emsim/assets/atom_params.txt")
 OUT = Path(__file__).with_name("kirkland_fe_params.csv")
 
 
-def main(src: Path = DEFAULT_SRC) -> None:
+def main(src: Path) -> None:
     lines = src.read_text().splitlines()
     rows = []
     for z in range(1, 104):
@@ -43,4 +42,6 @@ def main(src: Path = DEFAULT_SRC) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_SRC)
+    if len(sys.argv) != 2:
+        raise SystemExit(__doc__)
+    main(Path(sys.argv[1]))

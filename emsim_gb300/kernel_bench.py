@@ -12,7 +12,9 @@ cases: step (multislice_propagate), space (space_propagate), lens (lens_propagat
 image (multislice_image: plane wave -> slices -> lens -> |psi|^2), slices
 (make_multi_slices), atoms (build_slices: slices straight from atoms, --atoms per image,
 uniform over the slab), blobs (build_slices of --batch seeded protein-like blobs of --atoms
-atoms in a 40 A sphere, as in the bench step), bin (bin_atoms_multi_slices).
+atoms in a 40 A sphere), bin (bin_atoms_multi_slices), slab (the amorphous-carbon slab of the
+bench's headline, 0.1 A^-3 C over --n x 0.1 A square, --slices slices of 0.5 A deep:
+build_slices straight from its atoms, then multislice_image at 300 keV, Cs 1.0 mm, Scherzer).
 """
 from __future__ import annotations
 
@@ -46,7 +48,7 @@ def _time(fn, reps: int, flush: torch.Tensor) -> float:
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="step",
-                    choices=["step", "space", "lens", "image", "slices", "atoms", "blobs", "bin"])
+                    choices=["step", "space", "lens", "image", "slices", "atoms", "blobs", "bin", "slab"])
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--slices", type=int, default=4)
@@ -146,6 +148,39 @@ def main(argv=None):
             fn()
         t = _time(fn, args.reps, flush)
         out.update(batch=B, atoms=N, slices=S, seconds=t, images_per_s=B / t, slices_per_s=B * S / t)
+    elif args.case == "slab":
+        from . import atoms as atm
+        from . import physics, pot, synth
+        d, dz, kev = 0.1, 0.5, 300.0
+        el, xyz0 = synth.carbon_slab(0, lateral=n * d, thickness=S * dz)
+        mol = atm.centralize(atm.AtomList(el, xyz0))
+        ns, _, _ = pot.finalize_slice_size(tuple(mol.space), (d, d), dz, (n, n), None)
+        b = backend.MultiSlicesBuilder([6], ns, n, n, dz, d, d)
+        wp = backend.WavePropagator(n, n, d, d, kev)
+        lam = physics.electron_wave_length_angstrom(kev)
+        df, ap = physics.scherzer_condition(lam, 1.0)
+        dfs = np.array([df])
+        N = int(len(el))
+        c = torch.from_numpy(np.ascontiguousarray(mol.coordinates, dtype=np.float32)).to(dev)
+        cn = torch.tensor([N], dtype=torch.int32, device=dev)
+        o = torch.empty((1, ns, n, n), dtype=torch.float32, device=dev)
+        w = torch.empty((1, n, n), dtype=torch.complex64, device=dev)
+        img = torch.empty((1, n, n), dtype=torch.float32, device=dev)
+        nbytes = int(_native.load().emsim_gb300_build_slices_workspace_size(b._plan.handle, N, 1))
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        build = lambda: _native.call("emsim_gb300_build_slices", b._plan.handle, P(c), N, P(cn), 1, P(o), P(ws),  # noqa
+                                     nbytes, st())
+        image = lambda: _native.call("emsim_gb300_multislice_image", wp._plan.handle, P(o), ns, ns * n * n, dz,  # noqa
+                                     20.0, 1.0, dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1, ap, P(img),
+                                     P(w), None, 1, st())
+        for _ in range(args.warmup):
+            build()
+            image()
+        tb = _time(build, args.reps, flush)
+        ti = _time(image, args.reps, flush)
+        out.update(atoms=N, slices=ns, build_seconds=tb, image_seconds=ti,
+                   build_algo_gbs=(16.0 * N + 4.0 * ns * n * n) / tb / 1e9,
+                   per_step_us=1e6 * ti / (ns + 0.5), step_algo_gbs=20.0 * n * n * ns / ti / 1e9)
     elif args.case == "atoms":
         zs = [6, 7, 8, 16]
         b = backend.MultiSlicesBuilder(zs, S, n, n, 2.0, 1.0, 1.0)

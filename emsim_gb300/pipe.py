@@ -15,6 +15,7 @@ from typing import List, Optional, Sequence, Tuple, Union
 import numpy as np
 import torch
 
+from . import _native
 from . import atoms as atm
 from . import backend, pot, tem, wave
 
@@ -370,8 +371,10 @@ class PendingImages:
         return self._out is not None or self._event.query()
 
     def result(self) -> List[np.ndarray]:
+        """The images; raises ``DeviceWaitTimeout`` when a kernel gave up a bounded wait."""
         if self._out is None:
             self._event.synchronize()
+            _native.raise_on_device_error()
             out: List = [None] * self._n
             for idx, h, _ in self._groups:
                 a = h.numpy()

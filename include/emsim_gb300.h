@@ -8,7 +8,10 @@
  * extension uses.  Every entry point returns EMSIM_GB300_OK (0) or an error code; the
  * message of the last failure on the calling thread is returned by
  * emsim_gb300_last_error().  Work is enqueued asynchronously on "stream"; nothing here
- * synchronises the device except plan creation.
+ * synchronises the device except plan creation.  Plans and the library's per-device state
+ * (twiddle table, error word, static buffers) belong to the device's primary context:
+ * after cudaDeviceReset of a device, create new plans and make no call that relies on
+ * state set up before the reset.
  *
  * Reference interfaces replaced (paths inside the emsim project):
  *   emsim::cuda::WavePropagator    emsim/backend/cuda_ext/src/WavePropagator.h:15-41,
@@ -50,6 +53,26 @@ const char* emsim_gb300_last_error(void);
  * (its results are then invalid).  No reference counterpart: the reference reports
  * CUDA errors on stderr only (WavePropagator.cu:18-20). */
 int emsim_gb300_check_device_error(int* code);
+
+/* Read the current device's error word without synchronising the device and without
+ * clearing it: kernels that have not finished are not reflected, so call it after the
+ * host has waited (event, stream or device synchronisation) for the work it checks.
+ * The word lives in mapped page-locked host memory.  No reference counterpart. */
+int emsim_gb300_peek_device_error(int* code);
+
+/* Limit (ns of GPU global time) of the bounded mbarrier waits of the TMA-pipelined and
+ * tensor-core passes, process-wide; at least 1 ms, default 2 s.  After a timed-out wait a
+ * kernel still waits at least the default for its own copy in flight before it exits.
+ * No reference counterpart. */
+int emsim_gb300_set_wait_limit_ns(unsigned long long ns);
+unsigned long long emsim_gb300_get_wait_limit_ns(void);
+
+/* Self-test of the timeout path: one CTA waits, bounded by limit_ns (1 us .. 2 s), on an
+ * mbarrier that nothing arrives at, records the timeout in the device error word exactly
+ * as a pipelined pass does, and writes 1 (the wait completed) or 0 (it gave up) to
+ * *completed (device int).  Nothing is in flight, so the context stays usable.
+ * No reference counterpart. */
+int emsim_gb300_wait_timeout_probe(unsigned long long limit_ns, int* completed, void* stream);
 
 /* ---------------------------------------------------------------------------------
  * Wave propagator.  Replaces WavePropagator(n1, n2, d1, d2, waveLength,
@@ -208,6 +231,8 @@ int emsim_gb300_band_limit_slices(const float* slices, int n_slices, int n1, int
  * exits.  All calls on a device share it and it keeps the last call's contents (nothing
  * in it needs to start at zero); calls that overlap on the GPU race on it.  The first
  * call on a device looks up the buffer's address; make it before any stream capture.
+ * Like every plan, that address is invalid after cudaDeviceReset of the device; do not
+ * call this on a device after resetting it.
  * ------------------------------------------------------------------------------- */
 #define EMSIM_GB300_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int emsim_gb300_make_slices_noalloc(emsim_gb300_slice_plan* plan, const float* hist, float* out, void* stream);

@@ -1,7 +1,9 @@
 """Import the reference emsim package (numpy backend) from its source tree.
 
 Test infrastructure only, and usable only where the reference tree exists (the
-development container; never a GPU host).  Two shims are needed to import it
+development container; never a GPU host).  Its location comes from the environment
+variable ``EMSIM_REFERENCE_ROOT`` (the fixture-generating scripts under ``tests/golden``
+set it).  Two shims are needed to import it
 unchanged:
 
 * ``emsim/utils/pdb.py:12-13`` imports Biopython at package import; Biopython is not
@@ -18,17 +20,21 @@ import tempfile
 import types
 from pathlib import Path
 
-REFERENCE_ROOT = Path(os.environ.get("EMSIM_REFERENCE_ROOT", "/root/reference"))
+def reference_root():
+    v = os.environ.get("EMSIM_REFERENCE_ROOT")
+    return Path(v) if v else None
 
 
 def available() -> bool:
-    return (REFERENCE_ROOT / "emsim" / "__init__.py").is_file()
+    root = reference_root()
+    return root is not None and (root / "emsim" / "__init__.py").is_file()
 
 
 def load():
     """Return the imported reference ``emsim`` package (numpy backend selected)."""
     if not available():
-        raise RuntimeError(f"reference emsim tree not found at {REFERENCE_ROOT}")
+        raise RuntimeError(f"reference emsim tree not found (EMSIM_REFERENCE_ROOT={reference_root()})")
+    REFERENCE_ROOT = reference_root()
     if "emsim" in sys.modules:
         return sys.modules["emsim"]
     sys.dont_write_bytecode = True

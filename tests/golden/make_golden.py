@@ -9,6 +9,7 @@ Usage:  python tests/golden/make_golden.py [generator ...]
 """
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -16,6 +17,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
+os.environ.setdefault("EMSIM_REFERENCE_ROOT", "/root/reference")
 
 from oracle import ref_numpy  # noqa: E402
 

@@ -321,3 +321,42 @@ def test_emsim_results_in_input_order_one_at_a_time_and_batched():
             assert fake.single == [4, 5, 6, 7, 8, 9, 10]  # the two failed groups, rerun one by one
     with pytest.raises(ValueError):
         EMSim(FakePipe(), mols, lambda *a: None, batch_size=0)
+
+
+def test_wait_limit_setting_host_side():
+    """emsim_gb300_set/get_wait_limit_ns store the bounded-wait limit without a GPU and
+    refuse limits below 1 ms (a pipelined kernel would give up on copies still landing)."""
+    lib = _native.load()
+    default = lib.emsim_gb300_get_wait_limit_ns()
+    assert default == 2_000_000_000
+    assert lib.emsim_gb300_set_wait_limit_ns(999_999) == 1
+    assert "1 ms" in _native.last_error()
+    assert lib.emsim_gb300_get_wait_limit_ns() == default
+    assert lib.emsim_gb300_set_wait_limit_ns(50_000_000) == 0
+    assert lib.emsim_gb300_get_wait_limit_ns() == 50_000_000
+    assert lib.emsim_gb300_set_wait_limit_ns(default) == 0
+    assert lib.emsim_gb300_wait_timeout_probe(10, None, None) == 1  # null output, limit below 1 us
+
+
+def test_frontend_trace_binds_to_backend_signatures():
+    """Every backend call that emsim's own front-end made (recorded from the reference
+    package: five atoms through pot.build_one_slice / TEM.get_wave_propagator /
+    init_wave / slice_transmit / lens_propagate, and Pipe.run of a blob) binds to the
+    GB300 backend's constructors and methods with the same arguments."""
+    import inspect
+
+    import frontend_trace
+    from emsim_gb300 import backend
+
+    trace, arrays = frontend_trace.load()
+    records = trace["records"]
+    assert {r["cls"] for r in records} == {"OneSliceBuilder", "MultiSlicesBuilder", "WavePropagator"}
+    assert {r["method"] for r in records if r["op"] == "call"} >= {
+        "bin_atoms_one_slice", "make_one_slice", "bin_atoms_multi_slices", "make_multi_slices", "init_wave",
+        "slice_transmit", "multislice_propagate", "lens_propagate"}
+    placeholder = object()
+    for r in records:
+        cls = getattr(backend, r["cls"])
+        fn = cls.__init__ if r["op"] == "new" else getattr(cls, r["method"])
+        args = [placeholder] + [placeholder] * len(r["args"])  # self + positional arguments
+        inspect.signature(fn).bind(*args, **{k: placeholder for k in r["kwargs"]})

@@ -37,11 +37,14 @@ def _plan(lib, zs, ns, n1, n2, d):
     return h
 
 
-def test_noalloc_matches_workspace_version_twice(lib):
+# 128 x 128 with 6 slices: power-of-two passes, every slice pair full; 96 x 80 with 5
+# slices: the generic (non-power-of-two) path and a half-empty last slice pair
+@pytest.mark.parametrize("ns,n1,n2", [(6, 128, 128), (5, 96, 80)])
+def test_noalloc_matches_workspace_version_twice(lib, ns, n1, n2):
     import torch
 
     from oracle import multislice as om
-    zs, ns, n1, n2 = [6, 7, 8, 16], 6, 128, 128
+    zs = [6, 7, 8, 16]
     plan = _plan(lib, zs, ns, n1, n2, 0.5)
     need = int(lib.emsim_gb300_make_slices_workspace_size(plan))
     assert 0 < need <= 32 * 1024 * 1024
