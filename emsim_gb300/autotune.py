@@ -118,11 +118,11 @@ def tune(n1: int, n2: int, batch: Optional[int] = None, n_slices: int = 6, reps:
     g1, g2 = get_tuning(n1), get_tuning(n2)
     best_t = float("inf")
     best_col = (g1["col_tma"], g1["col_cols"])
-    # column kernels: TMA radix-8 (-1), plain radix-8 (0) and, at length 256, TMA radix-16
-    # (2, 32 columns per tile by default)
+    # column kernels: TMA radix-8 (-1), plain radix-8 (0) and, at lengths 256..4096, TMA
+    # with 16 values per thread (2, 512 threads: 512 / (n1 / 16) columns per tile by default)
     col_kernels = {-1: (g1["default_col_cols_tma"], 2), 0: (g1["default_col_cols"], 1)}
-    if n1 == 256:
-        col_kernels[2] = (32, 2)
+    if 256 <= n1 <= 4096:
+        col_kernels[2] = (max(2, 512 // (n1 // 16)), 2)
     for tma, (default_cols, min_cols) in col_kernels.items():
         for cols in _halvings(default_cols, min_cols):
             _set_col(n1, tma, cols)
@@ -131,11 +131,11 @@ def tune(n1: int, n2: int, batch: Optional[int] = None, n_slices: int = 6, reps:
                 best_col, best_t = (tma, cols), t
     _set_col(n1, *best_col)
     best_row = (g2["row_tma"], g2["row_rows"])
-    # row kernels: TMA radix-8 (-1), plain radix-8 (0) and, at length 256, TMA radix-16 (2,
-    # 16 rows per tile by default)
+    # row kernels: TMA radix-8 (-1), plain radix-8 (0) and, at lengths 256..4096, TMA with 16
+    # values per thread (2, 256 threads: 256 / (n2 / 16) rows per tile by default)
     row_kernels = {-1: g2["default_row_rows_tma"], 0: g2["default_row_rows"]}
-    if n2 == 256:
-        row_kernels[2] = 16
+    if 256 <= n2 <= 4096:
+        row_kernels[2] = max(1, 256 // (n2 // 16))
     for tma, default_rows in row_kernels.items():
         for rows in _halvings(default_rows, 1):
             _set_row(n2, tma, rows)

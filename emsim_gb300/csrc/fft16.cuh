@@ -1,6 +1,8 @@
-// 256-point FFT as two radix-16 Stockham passes, 16 values per thread, 16 threads per
-// sequence: one shared-memory exchange per transform instead of the two of the radix-8
-// form (8 x 8 x 4), and no third pass.
+// FFTs with 16 values per thread.  Length 256: two radix-16 Stockham passes, 16 threads
+// per sequence, one shared-memory exchange per transform instead of the two of the
+// radix-8 form (8 x 8 x 4), and no third pass.  Lengths 512..4096 (fft16n): radix-16
+// passes then one radix-2/4/8 pass (2048 = 16 x 16 x 8: two exchanges instead of the
+// three of 8 x 8 x 8 x 4), N / 16 threads per sequence.
 //
 // Register contract (as fft_regs, with 16 values): thread t of a sequence holds
 // v[m] = x[t + 16 m] on entry and v[m] = X[t + 16 m] on return.  Pass 1 (stride 1) runs
@@ -29,6 +31,13 @@ constexpr int T = 16;
 // (p >> 4) & (16 / B - 1), which spreads the 16 / B positions a half-warp touches.
 struct RowSlot {
     __device__ __forceinline__ int operator()(int b, int p) const { return b * N + (p ^ ((p >> 4) & 15)); }
+};
+// The same row layout for any length L: the scatters of the radix-16 passes (positions
+// 16 j + r, and (j / 16) 256 + j % 16 + 16 r) and the contiguous gathers t + m T touch
+// distinct bank pairs within every half-warp.
+template <int L>
+struct RowSlotN {
+    __device__ __forceinline__ int operator()(int b, int p) const { return b * L + (p ^ ((p >> 4) & 15)); }
 };
 struct ColSlot {
     int B, mask;
@@ -118,6 +127,122 @@ __device__ __forceinline__ void fft256(float2 (&v)[16], float2* __restrict__ sm,
         v[8 + r] = cmul(v[8 + r], cmul(w8, wr));
     }
     dft16<INV>(v);
+}
+
+// ---- lengths 512..4096 -------------------------------------------------------------
+template <int L>
+struct Shape {
+    static constexpr int T = L / 16;                  // threads per sequence
+    static constexpr int LOG = fft::ilog2(L);
+    static constexpr int P16 = LOG / 4;              // radix-16 passes
+    static constexpr int REM = LOG - 4 * P16;        // last pass radix 2^REM (0: none)
+    static constexpr int NPASS = P16 + (REM ? 1 : 0);
+};
+
+// How the threads of one sequence synchronise around an exchange: within a warp, the
+// whole CTA, or a named barrier per sequence (id 1 + b, T threads; T a multiple of 32).
+enum SyncKind : int { SYNC_WARP = 0, SYNC_CTA = 1, SYNC_SEQ = 2 };
+
+template <int KIND, int TS>
+__device__ __forceinline__ void seq_sync(int b) {
+    if (KIND == SYNC_WARP) __syncwarp();
+    else if (KIND == SYNC_CTA) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"r"(1 + b), "r"(TS) : "memory");
+}
+
+// One radix-R Stockham pass (stride Ns) over the 16 register-held values: thread t runs
+// the 16 / R butterflies j = t + q T, whose inputs are its own positions; outputs go to
+// shared memory, or stay in registers (slot q + r 16 / R holds position j + r Ns) when
+// LAST.
+template <int L, int R, bool INV, bool LAST, bool TW_SMEM, class AddrF>
+__device__ __forceinline__ void pass(float2 (&v)[16], int Ns, float2* __restrict__ sm, int b, int t, AddrF addr,
+                                     const float2* __restrict__ tw) {
+    constexpr int T = L / 16;
+    constexpr int Q = 16 / R;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int j = t + q * T;
+        const int k = j & (Ns - 1);
+        float2 x[16];
+#pragma unroll
+        for (int r = 0; r < R; ++r) x[r] = v[q + r * Q];
+        if (Ns > 1) {
+            const int stride = fft::TW_SIZE / (Ns * R);
+            const float2 w1 = fft::twiddle<INV, TW_SMEM>(tw, k * stride);
+            if (R == 16) {
+                // W^k and W^(8k) from the table, the other powers as running products
+                const float2 w8 = fft::twiddle<INV, TW_SMEM>(tw, 8 * k * stride);
+                x[8] = cmul(x[8], w8);
+                float2 wr = w1;
+#pragma unroll
+                for (int r = 1; r < 8; ++r) {
+                    if (r > 1) wr = cmul(wr, w1);
+                    x[r] = cmul(x[r], wr);
+                    x[8 + r] = cmul(x[8 + r], cmul(w8, wr));
+                }
+            } else {
+                x[1] = cmul(x[1], w1);
+                if (R >= 4) {
+                    const float2 w2 = cmul(w1, w1);
+                    const float2 w3 = cmul(w2, w1);
+                    x[2] = cmul(x[2], w2);
+                    x[3] = cmul(x[3], w3);
+                    if (R == 8) {
+                        const float2 w4 = cmul(w2, w2);
+                        x[4] = cmul(x[4], w4);
+                        x[5] = cmul(x[5], cmul(w4, w1));
+                        x[6] = cmul(x[6], cmul(w4, w2));
+                        x[7] = cmul(x[7], cmul(w4, w3));
+                    }
+                }
+            }
+        }
+        if (R == 16) dft16<INV>(x);
+        else if (R == 8) fft::dft8<INV>(x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7]);
+        else if (R == 4) fft::dft4<INV>(x[0], x[1], x[2], x[3]);
+        else fft::dft2<INV>(x[0], x[1]);
+        if (LAST) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[q + r * Q] = x[r];
+        } else {
+            const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) sm[addr(b, base + r * Ns)] = x[r];
+        }
+    }
+}
+
+// Length-L transform (512 <= L <= 4096) of the register-held sequence: thread t holds
+// x[t + m L / 16] on entry and X[t + m L / 16] on return.  Every thread of the sequence
+// (of the CTA for SYNC_CTA) calls it; the exchange slots are free on entry and on return.
+// Unnormalised both ways.
+template <int L, bool INV, int SYNC, bool TW_SMEM = false, class AddrF>
+__device__ __forceinline__ void fft16n(float2 (&v)[16], float2* __restrict__ sm, int b, int t, AddrF addr,
+                                       const float2* __restrict__ tw) {
+    using S = Shape<L>;
+    static_assert(L >= 512 && L <= fft::TW_SIZE && (L & (L - 1)) == 0, "power-of-two length 512..4096");
+    int Ns = 1;
+#pragma unroll
+    for (int p = 0; p < S::NPASS; ++p) {
+        if (p > 0) {
+#pragma unroll
+            for (int m = 0; m < 16; ++m) v[m] = sm[addr(b, t + m * S::T)];
+            seq_sync<SYNC, S::T>(b);
+        }
+        const bool last = (p == S::NPASS - 1);
+        if (p < S::P16) {
+            if (last) pass<L, 16, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+            else pass<L, 16, INV, false, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+            Ns *= 16;
+        } else if (S::REM == 3) {
+            pass<L, 8, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+        } else if (S::REM == 2) {
+            pass<L, 4, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+        } else {
+            pass<L, 2, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+        }
+        if (!last) seq_sync<SYNC, S::T>(b);
+    }
 }
 
 }  // namespace fft16

