@@ -455,11 +455,11 @@ def plain_cufft_extra(torch, db: DeviceImages, flush, reps: int = 3) -> dict:
             "speedup": round(t_plain / t_fused, 3), "rel_l2_plain_vs_fused": rel}
 
 
-def batching_extra(torch, p, n_blobs: int = 32, reps: int = 2) -> dict:
-    """A mixed batch through Pipe.run_batch: blobs with log-uniform 5k-200k atoms at
-    0.1 A^-3, random orientations, roi 256 or 512, every other one in amorphous ice;
-    wall clock from host atoms to device images (ragged slice counts, two lateral sizes
-    on two streams)."""
+def batching_extra(torch, p, n_blobs: int = 256, reps: int = 2) -> dict:
+    """The batching workload through Pipe.run_batch: 256 blobs with log-uniform 5k-200k
+    atoms at 0.1 A^-3, random orientations, roi 256 or 512, every other one in amorphous
+    ice; wall clock from host atoms to device images (ragged slice counts, two lateral
+    sizes on two streams, two chunks)."""
     from emsim_gb300 import atoms, synth
     mix = synth.batching_mix(n_blobs, seed=11, pixel=0.5 * BLOB["resolution"])
     mols = [atoms.AtomList(el, xyz) for el, xyz, _ in mix]

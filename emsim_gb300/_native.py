@@ -57,6 +57,10 @@ SIGNATURES = {
     "emsim_gb300_centralize": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "emsim_gb300_build_slices_z": (_c_int, [_c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_int,
                                             _c_vp, _c_vp, _c_size, _c_vp]),
+    "emsim_gb300_image_from_atoms_workspace_size": (_c_size, [_c_vp, _c_uint, _c_int, _c_int]),
+    "emsim_gb300_image_from_atoms_z": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,
+                                                _c_int, _c_dbl, _c_dbl, ctypes.POINTER(ctypes.c_double), _c_int,
+                                                _c_dbl, _c_vp, _c_int, _c_vp, _c_size, _c_vp]),
     "emsim_gb300_smooth_workspace_size": (_c_size, [_c_vp, _c_uint, _c_int]),
     "emsim_gb300_build_slices_smooth": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
     "emsim_gb300_build_slices_smooth_adjoint": (_c_int, [_c_vp, _c_vp, _c_uint, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,

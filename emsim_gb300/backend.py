@@ -268,6 +268,38 @@ def build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tenso
     return _wrap(out)
 
 
+def image_from_device_atoms(builder: MultiSlicesBuilder, wp: "WavePropagator", xyz: torch.Tensor, z: torch.Tensor,
+                            offsets: torch.Tensor, shift: torch.Tensor, mol_index: Sequence[int], n_mol: int,
+                            electron_dose: float, cs_mm: float, defocus, aperture: float,
+                            chunk_pairs: int = 0) -> DeviceArray:
+    """Images of molecules ``mol_index`` of a device-resident batch (arguments as for
+    :func:`build_slices_from_device_atoms`) with the slices built ``chunk_pairs`` slice
+    pairs at a time (``emsim_gb300_image_from_atoms_z``): the slice stack is never held
+    whole, and the images are bitwise those of build_slices_from_device_atoms followed
+    by ``WavePropagator.image``.  Returns (len(mol_index), n1, n2) float32."""
+    plan = builder._plan
+    dev = _device()
+    slot = np.full(n_mol, -1, dtype=np.int32)
+    slot[list(mol_index)] = np.arange(len(mol_index), dtype=np.int32)
+    eoz = np.full(128, -1, dtype=np.int32)
+    for k, zz in enumerate(sorted(int(v) for v in builder.unique_elements)):
+        if 0 <= zz < 128:
+            eoz[zz] = k
+    nb = len(mol_index)
+    meta = torch.from_numpy(np.concatenate([slot, eoz])).to(dev, non_blocking=True)
+    n_atoms = int(xyz.shape[0])
+    lib = _native.load()
+    nbytes = int(lib.emsim_gb300_image_from_atoms_workspace_size(plan.handle, n_atoms, nb, int(chunk_pairs)))
+    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+    img = torch.empty((nb, builder.n1, builder.n2), dtype=torch.float32, device=dev)
+    dfs = np.atleast_1d(np.asarray(defocus, dtype=np.float64))
+    _native.call("emsim_gb300_image_from_atoms_z", plan.handle, wp._plan.handle, _ptr(xyz), _ptr(z), n_atoms,
+                 _ptr(offsets), n_mol, _ptr(shift), _ptr(meta), ctypes.c_void_p(meta.data_ptr() + 4 * n_mol), nb,
+                 float(electron_dose), float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(dfs),
+                 float(aperture), _ptr(img), int(chunk_pairs), _ptr(ws), nbytes, _stream())
+    return _wrap(img)
+
+
 def build_slices_batch(builder: MultiSlicesBuilder, mols, symmetric_bandlimit: bool = True) -> DeviceArray:
     """Slices of several molecules in one engine call.  ``mols``: sequence of
     (coordinates sorted by element (N_b, 3), per-element counts in the builder's

@@ -15,6 +15,8 @@
 //   C  rows   : W[pair] -> inverse row FFT -> clip(re) -> V[2p], clip(im) -> V[2p+1]
 #pragma once
 
+#include <cstdlib>
+
 #include "fft16.cuh"
 #include "slices.h"
 #include "wave_passes.cuh"
@@ -98,9 +100,9 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     const int b = threadIdx.x & (B - 1);
     const int t = threadIdx.x / B;
     const int col = blockIdx.x * B + b;
-    const int y = blockIdx.y;  // img * n_pairs + pair
-    const int img = y / a.n_pairs;
-    const int pair = y - img * a.n_pairs;
+    const int y = blockIdx.y;  // img * pairs_here + pair - pair0
+    const int img = y / a.pairs_here();
+    const int pair = a.pair0 + (y - img * a.pairs_here());
     if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
     const long long npix = (long long)N * a.n2;
     const long long ld = a.n2;
@@ -112,14 +114,14 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
         return;
     }
     ColAddrRt addr{B};
-    // W_n2 table (even slice, then times i for the odd slice), padded by one entry every
-    // 16: the lookups (j * col) mod n2 of the B consecutive columns of a row have stride j,
-    // which the padding spreads over the banks
+    // W_n2 table, padded by one entry every 16: the lookups (j * col) mod n2 of the B
+    // consecutive columns of a row have stride j, which the padding spreads over the banks.
+    // The odd slice of a pair takes i W^m = (-sin, cos), exactly the integers of W^m.
     int2* wq = reinterpret_cast<int2*>(sm + (N + N / 8) * B);
-    for (int i = threadIdx.x; i < 2 * a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
+    for (int i = threadIdx.x; i < a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
     // the plane's bucket offsets and (up to ITEM_CACHE) items, staged in shared memory by
     // coalesced loads: the sums below then wait on shared, not global, memory per atom
-    unsigned* s_off = reinterpret_cast<unsigned*>(wq + 2 * a.n2 + a.n2 / 8 + 1);
+    unsigned* s_off = reinterpret_cast<unsigned*>(wq + a.n2 + a.n2 / 16 + 1);
     unsigned* s_items = s_off + N + 1;
     __syncthreads();
     constexpr float INV_SCALE = (float)(1.0 / WQ_SCALE);
@@ -149,21 +151,22 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
                 int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
                 for (unsigned k = lo; k < hi; ++k) {
                     const unsigned u = items[k];
-                    // the odd slice of the pair reads the i W half of the table
-                    const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
+                    const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
                     const int2 w = wq[idx + (idx >> 4)];
-                    re += w.x;
-                    im += w.y;
+                    const bool odd = (u >> 31) != 0;  // the odd slice of the pair: i W^m
+                    re += odd ? -w.y : w.x;
+                    im += odd ? w.x : w.y;
                 }
                 v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
             } else {
                 long long re = 0, im = 0;
                 for (unsigned k = lo; k < hi; ++k) {
                     const unsigned u = items[k];
-                    const int idx = (((int)(u & 0x7fffffffu) * col) & kmask) + (int)(u >> 31) * a.n2;
+                    const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
                     const int2 w = wq[idx + (idx >> 4)];
-                    re += w.x;
-                    im += w.y;
+                    const bool odd = (u >> 31) != 0;
+                    re += odd ? -w.y : w.x;
+                    im += odd ? w.x : w.y;
                 }
                 v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
             }
@@ -186,11 +189,15 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
 template <int N>
 int slice_cols_atoms_n(const SliceArgs& a, cudaStream_t st) {
     constexpr int T = N / 8;
-    const int B = col_B_for(N, a.n2);
-    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(2 * a.n2 + a.n2 / 8 + 1) * sizeof(int2) +
+    int B = col_B_for(N, a.n2);
+    if (const char* e = std::getenv("EMSIM_GB300_SLICE_COLS_B")) {
+        const int v = std::atoi(e);
+        if (v >= 1 && v <= B && (v & (v - 1)) == 0) B = v;
+    }
+    const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) +
                         (size_t)(N + 1 + ITEM_CACHE) * sizeof(unsigned);
     EMSIM_TRY(ensure_smem_attr((const void*)slice_cols_atoms_kernel<N>, smem));
-    slice_cols_atoms_kernel<N><<<dim3(a.n2 / B, a.n_img * a.n_pairs), B * T, smem, st>>>(a);
+    slice_cols_atoms_kernel<N><<<dim3(a.n2 / B, a.n_img * a.pairs_here()), B * T, smem, st>>>(a);
     EMSIM_CHECK_LAUNCH();
     return EMSIM_GB300_OK;
 }
@@ -206,9 +213,10 @@ __global__ void __launch_bounds__(512) slice_rows_inv_kernel(SliceArgs a) {
     const int t = threadIdx.x - b * T;
     const int B = blockDim.x / T;
     const int row = blockIdx.x * B + b;
-    const int y = blockIdx.y;  // img * n_pairs + pair
-    const int img = y / a.n_pairs;
-    const int pair = y - img * a.n_pairs;
+    const int y = blockIdx.y;  // img * pairs_here + pair - pair0
+    const int img = y / a.pairs_here();
+    const int local = y - img * a.pairs_here();
+    const int pair = a.pair0 + local;
     if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
     const long long npix = (long long)a.n1 * N;
     const float2* src = a.work + (long long)y * npix + (long long)row * N;
@@ -216,13 +224,12 @@ __global__ void __launch_bounds__(512) slice_rows_inv_kernel(SliceArgs a) {
 #pragma unroll
     for (int m = 0; m < 8; ++m) v[m] = src[t + m * T];
     fft::fft_regs<N, true, WARP_ONLY>(v, sm, b, t, RowAddr<N>{}, a.tw);
-    const int s0 = 2 * pair, s1 = 2 * pair + 1;
-    float* out = a.out + (long long)img * a.n_slices * npix;
-    float* o0 = out + (long long)s0 * npix + (long long)row * N;
+    float* out = a.out + (long long)img * a.out_stride_slices() * npix;
+    float* o0 = out + (long long)(2 * local) * npix + (long long)row * N;
 #pragma unroll
     for (int m = 0; m < 8; ++m) o0[t + m * T] = clip_low(v[m].x);
-    if (s1 < a.n_slices) {
-        float* o1 = out + (long long)s1 * npix + (long long)row * N;
+    if (2 * pair + 1 < a.n_slices) {
+        float* o1 = out + (long long)(2 * local + 1) * npix + (long long)row * N;
 #pragma unroll
         for (int m = 0; m < 8; ++m) o1[t + m * T] = clip_low(v[m].y);
     }
@@ -255,9 +262,10 @@ __global__ void __launch_bounds__(256) slice_rows_inv16_kernel(SliceArgs a) {
     const int t = threadIdx.x - b * T;
     const int B = blockDim.x / T;
     const int row = blockIdx.x * B + b;
-    const int y = blockIdx.y;  // img * n_pairs + pair
-    const int img = y / a.n_pairs;
-    const int pair = y - img * a.n_pairs;
+    const int y = blockIdx.y;  // img * pairs_here + pair - pair0
+    const int img = y / a.pairs_here();
+    const int local = y - img * a.pairs_here();
+    const int pair = a.pair0 + local;
     if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
     const long long npix = (long long)a.n1 * N;
     const float2* src = a.work + (long long)y * npix + (long long)row * N;
@@ -265,13 +273,12 @@ __global__ void __launch_bounds__(256) slice_rows_inv16_kernel(SliceArgs a) {
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = src[t + m * T];
     fft16::fft256<true, true>(v, sm, b, t, fft16::RowSlot{}, a.tw);
-    const int s0 = 2 * pair, s1 = 2 * pair + 1;
-    float* out = a.out + (long long)img * a.n_slices * npix;
-    float* o0 = out + (long long)s0 * npix + (long long)row * N;
+    float* out = a.out + (long long)img * a.out_stride_slices() * npix;
+    float* o0 = out + (long long)(2 * local) * npix + (long long)row * N;
 #pragma unroll
     for (int m = 0; m < 16; ++m) o0[t + m * T] = clip_low(v[m].x);
-    if (s1 < a.n_slices) {
-        float* o1 = out + (long long)s1 * npix + (long long)row * N;
+    if (2 * pair + 1 < a.n_slices) {
+        float* o1 = out + (long long)(2 * local + 1) * npix + (long long)row * N;
 #pragma unroll
         for (int m = 0; m < 16; ++m) o1[t + m * T] = clip_low(v[m].y);
     }
@@ -283,11 +290,11 @@ int slice_rows_inv_n(const SliceArgs& a, cudaStream_t st) {
         const int B = 16;  // rows per CTA, 256 threads
         const size_t smem = (size_t)B * N * sizeof(float2);
         EMSIM_TRY(ensure_smem_attr((const void*)slice_rows_inv16_kernel, smem));
-        slice_rows_inv16_kernel<<<dim3(a.n1 / B, a.n_img * a.n_pairs), B * fft16::T, smem, st>>>(a);
+        slice_rows_inv16_kernel<<<dim3(a.n1 / B, a.n_img * a.pairs_here()), B * fft16::T, smem, st>>>(a);
         EMSIM_CHECK_LAUNCH();
         return EMSIM_GB300_OK;
     }
-    return rows_launch<N>(slice_rows_inv_kernel<N>, a, a.n1, a.n_img * a.n_pairs, st);
+    return rows_launch<N>(slice_rows_inv_kernel<N>, a, a.n1, a.n_img * a.pairs_here(), st);
 }
 // Pass B on columns of length n1 (= N here)
 template <int N>

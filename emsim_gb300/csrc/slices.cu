@@ -11,6 +11,7 @@
 #include "binning.cuh"
 #include "slice_plan.h"
 #include "slices.h"
+#include "wave_plan.h"
 
 using namespace emsim_gb300;
 
@@ -224,10 +225,12 @@ struct AtomsWorkspace {
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-AtomsWorkspace atoms_workspace(const emsim_gb300_slice_plan* p, unsigned n_atoms, int n_img) {
+// work_pairs: slice pairs per image held in the complex work buffer (-1: all of them)
+AtomsWorkspace atoms_workspace(const emsim_gb300_slice_plan* p, unsigned n_atoms, int n_img, long long work_pairs = -1) {
     AtomsWorkspace w;
     const long long n_groups = (long long)n_img * p->n_elems;
     const long long pairs = (p->n_slices + 1) / 2;
+    if (work_pairs < 0 || work_pairs > pairs) work_pairs = pairs;
     w.n_buckets = n_groups * pairs * p->n1;
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -244,9 +247,59 @@ AtomsWorkspace atoms_workspace(const emsim_gb300_slice_plan* p, unsigned n_atoms
     w.cursor = take(sizeof(unsigned) * (size_t)w.n_buckets);
     w.bucket_tmp = take(sizeof(unsigned) * scan_tmp_words(w.n_buckets));
     w.items = take(sizeof(unsigned) * (size_t)n_atoms);
-    w.work = take(sizeof(float2) * (size_t)n_img * pairs * p->n1 * p->n2);
+    w.work = take(sizeof(float2) * (size_t)n_img * work_pairs * p->n1 * p->n2);
     w.total = o;
     return w;
+}
+
+// Counting sort of molecules given with atomic numbers (build_slices_z / _ragged and the
+// chunked image) into the workspace's buckets; fills the bucket fields of a.
+int bucket_atoms_z(emsim_gb300_slice_plan* p, const float* coords, const int32_t* z, unsigned n_atoms,
+                   const uint32_t* atom_offsets, int n_mol, const float* shift, const int32_t* mol_slot,
+                   const int32_t* elem_of_z, const int32_t* slot_slices, char* base, const AtomsWorkspace& w,
+                   SliceArgs& a, cudaStream_t st) {
+    auto U = [&](size_t off) { return reinterpret_cast<unsigned*>(base + off); };
+    const long long pairs = (p->n_slices + 1) / 2;
+    EMSIM_CHECK_CUDA(cudaMemsetAsync(U(w.count), 0, sizeof(unsigned) * (size_t)w.n_buckets, st));
+    AtomBucketZArgs ba;
+    ba.coords = coords;
+    ba.z = z;
+    ba.n_atoms = n_atoms;
+    ba.atom_offsets = atom_offsets;
+    ba.n_mol = n_mol;
+    ba.shift = shift;
+    ba.mol_slot = mol_slot;
+    ba.elem_of_z = elem_of_z;
+    ba.n_elems = p->n_elems;
+    ba.n_pairs = (int)pairs;
+    ba.n1 = p->n1;
+    ba.ax0 = make_axis(p->n_slices, p->dz);
+    ba.ax1 = make_axis(p->n1, p->d1);
+    ba.ax2 = make_axis(p->n2, p->d2);
+    ba.slot_slices = slot_slices;
+    ba.bucket = U(w.bucket);
+    ba.item = U(w.item);
+    ba.bucket_count = U(w.count);
+    EMSIM_TRY(atoms_bucket_z(ba, st));
+    EMSIM_TRY(scan_u32(U(w.count), U(w.off), w.n_buckets, U(w.bucket_tmp), st));
+    EMSIM_CHECK_CUDA(cudaMemcpyAsync(U(w.cursor), U(w.off), sizeof(unsigned) * (size_t)w.n_buckets,
+                                     cudaMemcpyDeviceToDevice, st));
+    EMSIM_TRY(atoms_scatter(U(w.bucket), U(w.item), n_atoms, U(w.cursor), U(w.items), st));
+    a.work = reinterpret_cast<float2*>(base + w.work);
+    a.filt = p->filt;
+    a.tw = p->tw;
+    a.n_elems = p->n_elems;
+    a.n_slices = p->n_slices;
+    a.n_pairs = (int)pairs;
+    a.n1 = p->n1;
+    a.n2 = p->n2;
+    a.bucket_off = U(w.off);
+    a.items = U(w.items);
+    a.wq = p->wq;
+    a.live_lo = p->col_cut + 1;
+    a.live_hi = p->col_cut > 0 ? p->col_cut : 0;
+    a.img_slices = slot_slices;
+    return EMSIM_GB300_OK;
 }
 
 }  // namespace
@@ -467,51 +520,119 @@ int emsim_gb300_build_slices_ragged(emsim_gb300_slice_plan* p, const float* coor
     EMSIM_REQUIRE((long long)n_batch * pairs <= 65535, EMSIM_GB300_ERR_UNSUPPORTED,
                   "build_slices_z: more than 65535 image x slice-pair planes per call");
     cudaStream_t st = (cudaStream_t)stream;
-    char* base = (char*)workspace;
-    auto U = [&](size_t off) { return reinterpret_cast<unsigned*>(base + off); };
-    EMSIM_CHECK_CUDA(cudaMemsetAsync(U(w.count), 0, sizeof(unsigned) * (size_t)w.n_buckets, st));
-    AtomBucketZArgs ba;
-    ba.coords = coords;
-    ba.z = z;
-    ba.n_atoms = n_atoms;
-    ba.atom_offsets = atom_offsets;
-    ba.n_mol = n_mol;
-    ba.shift = shift;
-    ba.mol_slot = mol_slot;
-    ba.elem_of_z = elem_of_z;
-    ba.n_elems = p->n_elems;
-    ba.n_pairs = (int)pairs;
-    ba.n1 = p->n1;
-    ba.ax0 = make_axis(p->n_slices, p->dz);
-    ba.ax1 = make_axis(p->n1, p->d1);
-    ba.ax2 = make_axis(p->n2, p->d2);
-    ba.slot_slices = slot_slices;
-    ba.bucket = U(w.bucket);
-    ba.item = U(w.item);
-    ba.bucket_count = U(w.count);
-    EMSIM_TRY(atoms_bucket_z(ba, st));
-    EMSIM_TRY(scan_u32(U(w.count), U(w.off), w.n_buckets, U(w.bucket_tmp), st));
-    EMSIM_CHECK_CUDA(cudaMemcpyAsync(U(w.cursor), U(w.off), sizeof(unsigned) * (size_t)w.n_buckets,
-                                     cudaMemcpyDeviceToDevice, st));
-    EMSIM_TRY(atoms_scatter(U(w.bucket), U(w.item), n_atoms, U(w.cursor), U(w.items), st));
     SliceArgs a;
+    EMSIM_TRY(bucket_atoms_z(p, coords, z, n_atoms, atom_offsets, n_mol, shift, mol_slot, elem_of_z, slot_slices,
+                             (char*)workspace, w, a, st));
     a.out = out;
-    a.work = reinterpret_cast<float2*>(base + w.work);
-    a.filt = p->filt;
-    a.tw = p->tw;
-    a.n_elems = p->n_elems;
-    a.n_slices = p->n_slices;
-    a.n_pairs = (int)pairs;
-    a.n1 = p->n1;
-    a.n2 = p->n2;
     a.n_img = n_batch;
-    a.bucket_off = U(w.off);
-    a.items = U(w.items);
-    a.wq = p->wq;
-    a.live_lo = p->col_cut + 1;
-    a.live_hi = p->col_cut > 0 ? p->col_cut : 0;
-    a.img_slices = slot_slices;
     return slice_atoms_build(a, st);
+}
+
+// ---- image straight from atoms, slices built chunk by chunk ----------------------------
+namespace {
+
+struct ImageAtomsWorkspace {
+    AtomsWorkspace atoms;  // buckets and the chunk's complex work buffer
+    size_t slices, wave, total;
+};
+
+ImageAtomsWorkspace image_atoms_workspace(const emsim_gb300_slice_plan* p, unsigned n_atoms, int n_img,
+                                          int chunk_pairs) {
+    ImageAtomsWorkspace w;
+    w.atoms = atoms_workspace(p, n_atoms, n_img, chunk_pairs);
+    const size_t npix = (size_t)p->n1 * p->n2;
+    size_t o = w.atoms.total;
+    w.slices = o;
+    o = align256(o + sizeof(float) * (size_t)n_img * 2 * chunk_pairs * npix);
+    w.wave = o;
+    o = align256(o + sizeof(float2) * (size_t)n_img * npix);
+    w.total = o;
+    return w;
+}
+
+int chunk_of(const emsim_gb300_slice_plan* p, int chunk_pairs) {
+    const int pairs = (p->n_slices + 1) / 2;
+    return chunk_pairs < 1 || chunk_pairs > pairs ? pairs : chunk_pairs;
+}
+
+}  // namespace
+
+size_t emsim_gb300_image_from_atoms_workspace_size(const emsim_gb300_slice_plan* p, unsigned n_atoms, int n_batch,
+                                                   int chunk_pairs) {
+    if (!p || n_batch < 1) return 0;
+    return image_atoms_workspace(p, n_atoms, n_batch, chunk_of(p, chunk_pairs)).total;
+}
+
+int emsim_gb300_image_from_atoms_z(emsim_gb300_slice_plan* p, emsim_gb300_wave_plan* wp, const float* coords,
+                                   const int32_t* z, unsigned n_atoms, const uint32_t* atom_offsets, int n_mol,
+                                   const float* shift, const int32_t* mol_slot, const int32_t* elem_of_z, int n_batch,
+                                   double dose, double cs_mm, const double* defocus, int n_defocus, double aperture,
+                                   float* image_out, int chunk_pairs, void* workspace, size_t workspace_bytes,
+                                   void* stream) {
+    EMSIM_TRY(check_device(p));
+    EMSIM_TRY(check_device(wp));
+    EMSIM_REQUIRE(p->fast && wp->fast, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "image_from_atoms: sides must be powers of two in [8, 4096]");
+    EMSIM_REQUIRE(wp->n1 == p->n1 && wp->n2 == p->n2, EMSIM_GB300_ERR_INVALID,
+                  "image_from_atoms: wave plan and slice plan sizes differ");
+    EMSIM_REQUIRE(n_batch >= 1 && n_mol >= 1 && image_out && atom_offsets && shift && mol_slot && elem_of_z &&
+                      workspace && defocus && n_defocus >= 1 && ((coords && z) || n_atoms == 0),
+                  EMSIM_GB300_ERR_INVALID, "image_from_atoms: bad arguments");
+    const int chunk = chunk_of(p, chunk_pairs);
+    const ImageAtomsWorkspace w = image_atoms_workspace(p, n_atoms, n_batch, chunk);
+    EMSIM_REQUIRE(workspace_bytes >= w.total, EMSIM_GB300_ERR_INVALID, "image_from_atoms: workspace too small");
+    EMSIM_REQUIRE(((uintptr_t)workspace & 255) == 0, EMSIM_GB300_ERR_INVALID,
+                  "image_from_atoms: workspace not 256-byte aligned");
+    EMSIM_REQUIRE(w.atoms.n_buckets < (long long)INVALID_BUCKET, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "image_from_atoms: more than 2^32 - 1 (image, element, slice pair, row) buckets");
+    EMSIM_REQUIRE((long long)n_batch * chunk <= 65535, EMSIM_GB300_ERR_UNSUPPORTED,
+                  "image_from_atoms: more than 65535 image x slice-pair planes per chunk");
+    cudaStream_t st = (cudaStream_t)stream;
+    char* base = (char*)workspace;
+    SliceArgs a;
+    EMSIM_TRY(bucket_atoms_z(p, coords, z, n_atoms, atom_offsets, n_mol, shift, mol_slot, elem_of_z, nullptr, base,
+                             w.atoms, a, st));
+    float* slices = reinterpret_cast<float*>(base + w.slices);
+    float2* wave = reinterpret_cast<float2*>(base + w.wave);
+    a.out = slices;
+    a.n_img = n_batch;
+    a.out_slices = 2 * chunk;
+    const long long npix = (long long)p->n1 * p->n2;
+    const float4* p1;
+    const float2* p2;
+    EMSIM_TRY(get_prop(wp, p->dz, st, &p1, &p2));
+    RowArgs r = base_row(wp);
+    r.out = wave;
+    r.in = wave;
+    r.slice_img_stride = 2LL * chunk * npix;
+    r.const_val = make_float2((float)std::sqrt(dose * wp->d1 * wp->d2), 0.f);
+    ColArgs c = base_col(wp, wave);
+    c.p1 = p1;
+    c.p2 = p2;
+    for (int pair0 = 0; pair0 < a.n_pairs; pair0 += chunk) {
+        a.pair0 = pair0;
+        a.chunk_pairs = a.n_pairs - pair0 < chunk ? a.n_pairs - pair0 : chunk;
+        EMSIM_TRY(slice_atoms_build(a, st));
+        for (int s = 2 * pair0; s < p->n_slices && s < 2 * (pair0 + a.chunk_pairs); ++s) {
+            r.slice = slices + (long long)(s - 2 * pair0) * npix;
+            const int ops = s == 0 ? (ROW_CONST_IN | ROW_TRANSMIT | ROW_FFT) : (ROW_IFFT | ROW_TRANSMIT | ROW_FFT);
+            EMSIM_TRY(launch_row(p->n2, ops, r, n_batch, st));
+            EMSIM_TRY(launch_col(p->n1, COL_PROPAGATE, c, n_batch, st));
+        }
+    }
+    // FFT2(psi_exit) = n2 * FFT_cols(X): the lens acts on X directly with 1/n1
+    for (int i0 = 0; i0 < n_batch; i0 += LENS_MAX) {
+        const int cnt = n_batch - i0 < LENS_MAX ? n_batch - i0 : LENS_MAX;
+        ColArgs cl = base_col(wp, wave + i0 * npix);
+        set_lens(wp, cl, cs_mm, aperture, 1.0f / (float)p->n1);
+        cl.n_c2 = n_defocus == 1 ? 1 : cnt;
+        for (int j = 0; j < cl.n_c2; ++j) cl.c2v[j] = M_PI * wp->wave_length * defocus[(i0 + j) % n_defocus];
+        EMSIM_TRY(launch_col(p->n1, COL_LENS, cl, cnt, st));
+    }
+    RowArgs ri = base_row(wp);
+    ri.in = wave;
+    ri.out_int = image_out;
+    return launch_row(p->n2, ROW_IFFT | ROW_OUT_INTENSITY, ri, n_batch, st);
 }
 
 int emsim_gb300_make_slices(emsim_gb300_slice_plan* p, const float* hist, float* out, void* workspace,

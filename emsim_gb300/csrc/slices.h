@@ -21,6 +21,12 @@ struct SliceArgs {
     // columns [0, live_lo) and [n2 - live_hi, n2) hold the filters' support (T_e nonzero
     // for some element and row); every other column of the slice spectra is zero
     int live_lo = 0, live_hi = 0;
+    // chunked builds: this call covers slice pairs [pair0, pair0 + chunk_pairs) of every
+    // image (0: all n_pairs); work holds chunk_pairs pairs per image and out holds
+    // out_slices slices per image, slice 2 (pair - pair0) first (0: n_slices)
+    int pair0 = 0, chunk_pairs = 0, out_slices = 0;
+    __host__ __device__ int pairs_here() const { return chunk_pairs ? chunk_pairs : n_pairs; }
+    __host__ __device__ int out_stride_slices() const { return out_slices ? out_slices : n_slices; }
 };
 
 // fixed-point scale of the row-transform table: 511 entries sum below 2^31

@@ -17,13 +17,24 @@ import torch
 
 from . import _native
 from . import atoms as atm
-from . import backend, pot, tem, wave
+from . import backend, pot, shard, tem, wave
 
 
 # chunked run_batch: at least this many molecules and atoms per chunk, at most _MAX_CHUNKS
 _CHUNK_MIN_MOLS = 64
 _CHUNK_MIN_ATOMS = 1 << 21
 _MAX_CHUNKS = 2
+# a group whose slice stack would exceed this many bytes is imaged with its slices built
+# a few pairs at a time (emsim_gb300_image_from_atoms_z), in chunk buffers of about
+# _SLICE_CHUNK_BYTES; the images are bitwise the same
+_STACK_LIMIT_BYTES = 2 << 30
+_SLICE_CHUNK_BYTES = 256 << 20
+
+
+def slice_chunk_pairs(n_images: int, n1: int, n2: int) -> int:
+    """Slice pairs per chunk of the chunked image formation: the chunk's complex work and
+    its two float32 slices take 16 bytes per pixel per pair and image."""
+    return max(1, _SLICE_CHUNK_BYTES // (16 * n_images * n1 * n2))
 
 
 def _fast_len(n: int) -> bool:
@@ -199,6 +210,38 @@ class Pipe:
             ev.record(base)
         return PendingImages(len(mols), groups, ev)
 
+    def shard_costs(self, mols: Sequence[atm.AtomList], rois: Optional[Sequence] = None) -> List[float]:
+        """Estimated cost of each molecule's image - slices x pixels x log2(pixels), the FFT
+        work of its multislice loop - from the host coordinates' extent, which sizes its
+        stack exactly as the device front-end will (pot.finalize_slice_size)."""
+        costs = []
+        for i, mol in enumerate(mols):
+            lateral = self.roi if rois is None else (
+                (rois[i], rois[i]) if isinstance(rois[i], (int, np.integer)) else tuple(rois[i]))
+            ns, n1, n2 = pot.finalize_slice_size(tuple(mol.space), (self._pixel_size, self._pixel_size),
+                                                 self.slice_thickness, lateral, None)
+            costs.append(shard.image_cost(ns, n1, n2))
+        return costs
+
+    def run_sharded(self, mols: Sequence[atm.AtomList], defocus: Optional[Sequence[float]] = None,
+                    rois: Optional[Sequence] = None, group=None) -> Optional[List[np.ndarray]]:
+        """Images of many molecules over the ranks of a torch.distributed group, one GPU per
+        rank (emsim/simulator.py:64-91 spreads its work over threads of one process; here
+        over processes).  Every rank passes the same molecules; each images the share that
+        the deterministic cost partition (shard.partition: longest first, to the least
+        loaded rank) gives it with ``run_batch`` on its current device, and the host images
+        are gathered to rank 0 (torch.distributed.gather_object) - no collective touches the
+        device data.  Rank 0 returns the images in input order, the other ranks None."""
+        import torch.distributed as dist
+        rank, world = dist.get_rank(group), dist.get_world_size(group)
+        mine = shard.my_share(self.shard_costs(mols, rois), rank, world)
+        local = {}
+        if mine:
+            imgs = self.run_batch([mols[i] for i in mine], None if defocus is None else [defocus[i] for i in mine],
+                                  to_host=True, rois=None if rois is None else [rois[i] for i in mine])
+            local = {i: img for i, img in zip(mine, imgs)}
+        return shard.gather_to_root(local, len(mols), rank, world, group)
+
     def _queue_batch(self, mols, defocus, rois, main, slot) -> List:
         """Queue a batch's device work so that it completes in stream ``main``; returns
         [(indices, images)] with images (len(indices), n1, n2) on the device."""
@@ -296,12 +339,20 @@ class Pipe:
                                                self._pixel_size)
                 wp = self._propagator((n1, n2))
                 ragged = ss[0] != ss[-1]
-                if b.atoms_path:
+                # too large a stack to hold: slices built a few pairs at a time
+                chunked = b.atoms_path and not ragged and 4 * len(idx) * ss[0] * n1 * n2 > _STACK_LIMIT_BYTES
+                if chunked:
+                    imgs = backend.image_from_device_atoms(b, wp, xyz, zz, off, shift, idx, nm, m.electron_dose,
+                                                           m.cs_mm, dfs, m.aperture,
+                                                           slice_chunk_pairs(len(idx), n1, n2))
+                elif b.atoms_path:
                     stack = backend.build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, nm,
                                                                    slot_slices=ss if ragged else None)
                 else:
                     stack = torch.stack([self.build_slices(mols[i]) for i in idx])
-                if ragged:
+                if chunked:
+                    pass
+                elif ragged:
                     imgs = backend.image_ragged(wp, stack, ss, self.slice_thickness, m.electron_dose, m.cs_mm, dfs,
                                                 m.aperture)
                 else:

@@ -10,6 +10,11 @@ consumer groups that many molecules and keeps two groups in flight through
 Results still reach the handler in input order, one per molecule.  A group that fails
 as a whole is run again molecule by molecule, so only the failing molecules are
 reported, as with ``batch_size`` 1.
+
+``shard=(rank, world)`` (an addition): one process per GPU, each running its own EMSim
+over the same molecule source; rank r images the molecules i with i % world == r and
+hands them to its own handler.  A stream of unknown length cannot be partitioned by
+cost, so the split is round robin; ``Pipe.run_sharded`` balances a known list by cost.
 """
 from __future__ import annotations
 
@@ -34,9 +39,15 @@ class ImagePipeRunFailed(Exception):
 
 class EMSim:
     def __init__(self, image_pipe: pipe.Pipe, mols: Iterable[atm.AtomList], result_handler: Callable,
-                 batch_size: int = 1):
+                 batch_size: int = 1, shard=None):
         if batch_size < 1:
             raise ValueError("batch_size must be at least 1")
+        if shard is not None:
+            rank, world = (int(v) for v in shard)
+            if world < 1 or not 0 <= rank < world:
+                raise ValueError("shard must be (rank, world) with 0 <= rank < world")
+            shard = (rank, world)
+        self.shard = shard
         self.batch_size = int(batch_size)
         self.result_handler = result_handler
         self.image_pipe = image_pipe
@@ -75,9 +86,11 @@ class EMSim:
 
     def producer(self):
         try:
-            for mol in self.mols_iter:
+            for i, mol in enumerate(self.mols_iter):
                 if self.stop_event.is_set():
                     return
+                if self.shard is not None and i % self.shard[1] != self.shard[0]:
+                    continue  # another rank's molecule
                 self._task_q.put(mol)
         except Exception as e:  # a failing molecule source ends the run after reporting
             self._task_q.put(e)

@@ -260,6 +260,27 @@ int emsim_gb300_build_slices_z(emsim_gb300_slice_plan* plan, const float* coords
                                const int32_t* elem_of_z, int n_batch, float* out, void* workspace,
                                size_t workspace_bytes, void* stream);
 
+/* Image formation straight from atoms with the slices built chunk by chunk: Pipe.run
+ * without water (pipe.py:46-55, 79-84; pot.build_multi_slices pot.py:29-48, the slice
+ * builders SliceBuilder.cu:108-133 and the propagator WavePropagator.cu:14-70) for n_batch
+ * molecules of one element set and slice count, with memory O(chunk) instead of the
+ * (n_batch, n_slices, n1, n2) slice stack.  The atoms (as for emsim_gb300_build_slices_z)
+ * are bucketed once; then for each chunk of chunk_pairs slice pairs the slice passes fill
+ * a chunk buffer and the multislice steps (plane wave first, the wave plan's propagator
+ * for the slice plan's dz) run through it; last the lens and |psi|^2 into image_out
+ * (n_batch, n1, n2) float32.  Bitwise equal to emsim_gb300_build_slices_z followed by
+ * emsim_gb300_multislice_image.  chunk_pairs < 1 or above the pair count: one chunk.
+ * Both plans on the current device with equal sides, powers of two in [8, 4096]. */
+size_t emsim_gb300_image_from_atoms_workspace_size(const emsim_gb300_slice_plan* plan, unsigned n_atoms,
+                                                   int n_batch, int chunk_pairs);
+int emsim_gb300_image_from_atoms_z(emsim_gb300_slice_plan* plan, emsim_gb300_wave_plan* wave_plan,
+                                   const float* coords, const int32_t* z, unsigned n_atoms,
+                                   const uint32_t* atom_offsets, int n_mol, const float* shift,
+                                   const int32_t* mol_slot, const int32_t* elem_of_z, int n_batch,
+                                   double electron_dose, double cs_mm, const double* defocus_host, int n_defocus,
+                                   double aperture, float* image_out, int chunk_pairs, void* workspace,
+                                   size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------------------------------------------------
  * Off-grid ("smooth") slices and their coordinate adjoint.  No counterpart in the
  * reference, whose potential is piecewise constant in the atom positions because atoms
