@@ -233,6 +233,37 @@ def slab_step(torch, seed: int) -> DeviceImages:
                         SLAB["cs_mm"], df, ap)
 
 
+def chunked_extra(torch, seed: int, flush, reps: int = 3) -> dict:
+    """The headline image through emsim_gb300_image_from_atoms_z (slices built a few pairs
+    at a time, never the whole 6.7 GB stack) at 1 and 16 slice pairs per chunk, with the
+    device memory each needs; the images are bitwise those of the headline step."""
+    from emsim_gb300 import backend, pot
+    el, xyz = slab_atoms(seed)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    xyz_d = torch.from_numpy(xyz).to(dev)
+    z_d = torch.from_numpy(el.astype(np.int32)).to(dev)
+    off = torch.tensor([0, len(el)], dtype=torch.int32, device=dev)
+    shift = torch.empty((1, 3), dtype=torch.float32, device=dev)
+    space = torch.empty((1, 3), dtype=torch.float32, device=dev)
+    P = backend._ptr
+    backend._native.call("emsim_gb300_centralize", P(xyz_d), P(z_d), P(off), 1, P(shift), P(space), None,
+                         backend._stream())
+    n, d, dz = SLAB["n"], SLAB["pixel"], SLAB["dz"]
+    ns, _, _ = pot.finalize_slice_size(tuple(space.cpu().numpy()[0]), (d, d), dz, n, None)
+    b = backend.MultiSlicesBuilder([6], ns, n, n, dz, d, d)
+    wp = backend.WavePropagator(n, n, d, d, SLAB["kev"])
+    df, ap = scherzer()
+    lib = backend._native.load()
+    out = {"workload": "the headline image, slices built chunk by chunk (emsim_gb300_image_from_atoms_z)",
+           "whole_stack_bytes": 4 * ns * n * n}
+    for chunk in (1, 16):
+        t = timed(torch, lambda: backend.image_from_device_atoms(b, wp, xyz_d, z_d, off, shift, [0], 1, SLAB["dose"],
+                                                                 SLAB["cs_mm"], [df], ap, chunk), reps, flush)
+        out[f"pairs_{chunk}"] = {"images_per_s": round(1.0 / t, 3), "workspace_bytes": int(
+            lib.emsim_gb300_image_from_atoms_workspace_size(b._plan.handle, len(el), 1, chunk))}
+    return out
+
+
 def slice_step_on(torch, db: DeviceImages, peak_gbs: float, reps: int = 3, flush=None) -> dict:
     """Average duration of one slice step (fused row pass + column pass) of the step's
     own waves and slices: CUDA events around multislice_propagate through all slices of
@@ -629,6 +660,7 @@ def run_ours(args):
     plain = plain_cufft_extra(torch, db, flush)
     del db
     torch.cuda.empty_cache()
+    chunked = chunked_extra(torch, seed, flush)
 
     rl = {}
     for n, n_img, ns in [(256, 128, 40), (512, 32, 16), (2048, 2, 16)]:
@@ -671,6 +703,7 @@ def run_ours(args):
         "accuracy": {"blob_256": acc, "slab_2048": "tests/test_gpu_precision.py (FP64 oracle slab by slab)"},
         "precision": precision,
         "plain_cufft": plain,
+        "chunked_slices": chunked,
         "differentiation": diff,
         "batching": batching,
         "roofline": roofline,

@@ -155,6 +155,29 @@ int* error_word();
 // opt a kernel into more than 48 KB of dynamic shared memory (once per device)
 int ensure_smem_attr(const void* func, size_t smem_bytes);
 
+// Programmatic dependent launch of the persistent pass kernels (tma::pdl_wait): on for
+// eager launches unless the environment sets EMSIM_GB300_PDL=0; inside a stream capture
+// only with EMSIM_GB300_PDL=2 (in captured graphs it measured no faster).
+bool pdl_enabled(cudaStream_t st);
+
+// Launch k<<<grid, block, smem, st>>>(args...), with programmatic stream serialisation
+// when pdl_enabled(st): the kernel may start while its predecessor in the stream finishes
+// (it must call tma::pdl_wait() before touching the chain's global data).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_enabled(st) ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 // element-wise kernels (any size)
 int ew_transmit(const float2* in, const float* slice, float2* out, long long n, float sigma, int n_img,
                 long long in_stride, long long slice_stride, long long out_stride, cudaStream_t st);

@@ -15,8 +15,6 @@
 //   C  rows   : W[pair] -> inverse row FFT -> clip(re) -> V[2p], clip(im) -> V[2p+1]
 #pragma once
 
-#include <cstdlib>
-
 #include "fft16.cuh"
 #include "slices.h"
 #include "wave_passes.cuh"
@@ -189,11 +187,7 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
 template <int N>
 int slice_cols_atoms_n(const SliceArgs& a, cudaStream_t st) {
     constexpr int T = N / 8;
-    int B = col_B_for(N, a.n2);
-    if (const char* e = std::getenv("EMSIM_GB300_SLICE_COLS_B")) {
-        const int v = std::atoi(e);
-        if (v >= 1 && v <= B && (v & (v - 1)) == 0) B = v;
-    }
+    const int B = col_B_for(N, a.n2);
     const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) +
                         (size_t)(N + 1 + ITEM_CACHE) * sizeof(unsigned);
     EMSIM_TRY(ensure_smem_attr((const void*)slice_cols_atoms_kernel<N>, smem));

@@ -27,6 +27,17 @@ __device__ __forceinline__ void record_error(int* err, int code) {
     }
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialisation may start while the kernel before it in the stream still runs: it does
+// its set-up (barriers, shared-memory tables computed at plan creation), then pdl_wait()
+// blocks until every preceding kernel of the stream has completed and its writes are
+// visible, before any global data of the chain is read or written.  pdl_launch_dependents()
+// lets the next kernel of the stream launch early; it is called after pdl_wait(), so a
+// kernel that starts early knows that all kernels before its predecessor have completed.
+// Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

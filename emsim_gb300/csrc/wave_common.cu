@@ -99,6 +99,17 @@ bool tma_enabled() {
     return on;
 }
 
+bool pdl_enabled(cudaStream_t st) {
+    static const int mode = [] {
+        const char* v = std::getenv("EMSIM_GB300_PDL");
+        return v ? std::atoi(v) : 1;
+    }();
+    if (mode <= 0) return false;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return false;
+    return cap == cudaStreamCaptureStatusNone || mode >= 2;
+}
+
 static std::map<std::tuple<int, const void*, int, size_t>, int> g_occ;
 
 int persistent_grid(const void* func, int threads, size_t smem, int n_tiles) {

@@ -77,6 +77,9 @@ __global__ void __launch_bounds__(256, 2) row16_kernel(RowArgs a, int B, int til
         tma::fence_mbar_init();
     }
     __syncthreads();
+    // programmatic dependent launch: the chain's data is only touched after this point
+    tma::pdl_wait();
+    tma::pdl_launch_dependents();
     const bool pipelined = tx > 0;
     if (pipelined && tid == 0) {
         if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
@@ -181,6 +184,9 @@ __global__ void __launch_bounds__(512, 1)
         tma::fence_mbar_init();
     }
     __syncthreads();
+    // programmatic dependent launch: the chain's data is only touched after this point
+    tma::pdl_wait();
+    tma::pdl_launch_dependents();
     if (tid == 0) {
         if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
         if ((int)(blockIdx.x + gridDim.x) < n_tiles) issue(blockIdx.x + gridDim.x, 1);
@@ -266,7 +272,7 @@ bool launch_row16_n(int ops, const RowArgs& a, int n_img, cudaStream_t st, int* 
         *status = ensure_smem_attr(k, smem);                                                   \
         if (*status != EMSIM_GB300_OK) return true;                                            \
         const int grid = persistent_grid(k, threads, smem, n_tiles);                           \
-        r16::row16_kernel<L, OPS><<<grid, threads, smem, st>>>(a, B, tiles_per_img, n_tiles);  \
+        launch_pdl(r16::row16_kernel<L, OPS>, grid, threads, smem, st, a, B, tiles_per_img, n_tiles); \
         break;                                                                                 \
     }
         EMSIM_ROW16_CASE(ROW_FFT)
@@ -311,7 +317,8 @@ bool launch_col16_n(int mode, const ColArgs& a, int n_img, cudaStream_t st, int*
         *status = ensure_smem_attr(k, smem);                                                                 \
         if (*status != EMSIM_GB300_OK) return true;                                                          \
         const int grid = persistent_grid(k, threads, smem, tiles_per_img * n_img);                           \
-        r16::col16_kernel<L, MODE><<<grid, threads, smem, st>>>(map, a, B, tiles_per_img, lt.lo, lt.hi, n_img); \
+        launch_pdl(r16::col16_kernel<L, MODE>, grid, threads, smem, st, map, a, B, tiles_per_img, lt.lo, lt.hi,  \
+                   n_img);                                                                                   \
         break;                                                                                               \
     }
         EMSIM_COL16_CASE(COL_PROPAGATE)

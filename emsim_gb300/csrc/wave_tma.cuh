@@ -64,6 +64,9 @@ __global__ void __launch_bounds__(RowTma<N>::THREADS, RowTma<N>::MIN_BLOCKS)
         tma::fence_mbar_init();
     }
     __syncthreads();
+    // programmatic dependent launch: the chain's data is only touched after this point
+    tma::pdl_wait();
+    tma::pdl_launch_dependents();
     const bool pipelined = tx > 0;
     if (pipelined && tid == 0) {
         if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
@@ -205,6 +208,9 @@ __global__ void __launch_bounds__(512, 2)
         tma::fence_mbar_init();
     }
     __syncthreads();
+    // programmatic dependent launch: the chain's data is only touched after this point
+    tma::pdl_wait();
+    tma::pdl_launch_dependents();
     if (tid == 0) {
         if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
         if ((int)(blockIdx.x + gridDim.x) < n_tiles) issue(blockIdx.x + gridDim.x, 1);
@@ -285,7 +291,7 @@ int launch_row_tma_n(int ops, const RowArgs& a, int n_img, cudaStream_t st) {
         const void* k = (const void*)row_tma_kernel<N, OPS>;                                     \
         EMSIM_TRY(ensure_smem_attr(k, smem));                                                    \
         const int grid = persistent_grid(k, threads, smem, n_tiles);                             \
-        row_tma_kernel<N, OPS><<<grid, threads, smem, st>>>(a, B, tiles_per_img, n_tiles);       \
+        launch_pdl(row_tma_kernel<N, OPS>, grid, threads, smem, st, a, B, tiles_per_img, n_tiles); \
         break;                                                                                   \
     }
         EMSIM_ROW_TMA_CASE(ROW_FFT)
@@ -330,7 +336,7 @@ int launch_col_tma_n(int mode, const ColArgs& a, int n_img, cudaStream_t st) {
         const void* k = (const void*)col_tma_kernel<N, MODE>;                                    \
         EMSIM_TRY(ensure_smem_attr(k, smem));                                                    \
         const int grid = persistent_grid(k, threads, smem, tiles_per_img * n_img);               \
-        col_tma_kernel<N, MODE><<<grid, threads, smem, st>>>(map, a, B, tiles_per_img, lt.lo, lt.hi, n_img); \
+        launch_pdl(col_tma_kernel<N, MODE>, grid, threads, smem, st, map, a, B, tiles_per_img, lt.lo, lt.hi, n_img); \
         break;                                                                                   \
     }
         EMSIM_COL_TMA_CASE(COL_PROPAGATE)

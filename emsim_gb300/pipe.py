@@ -26,9 +26,10 @@ _CHUNK_MIN_ATOMS = 1 << 21
 _MAX_CHUNKS = 2
 # a group whose slice stack would exceed this many bytes is imaged with its slices built
 # a few pairs at a time (emsim_gb300_image_from_atoms_z), in chunk buffers of about
-# _SLICE_CHUNK_BYTES; the images are bitwise the same
+# _SLICE_CHUNK_BYTES; the images are bitwise the same.  Measured on the 2048^2 x 400-slice
+# slab: 16 pairs per chunk (1 GiB) cost 1.3 % against the whole 6.7 GB stack, 1 pair 12 %.
 _STACK_LIMIT_BYTES = 2 << 30
-_SLICE_CHUNK_BYTES = 256 << 20
+_SLICE_CHUNK_BYTES = 1 << 30
 
 
 def slice_chunk_pairs(n_images: int, n1: int, n2: int) -> int:
