@@ -360,3 +360,39 @@ def test_frontend_trace_binds_to_backend_signatures():
         fn = cls.__init__ if r["op"] == "new" else getattr(cls, r["method"])
         args = [placeholder] + [placeholder] * len(r["args"])  # self + positional arguments
         inspect.signature(fn).bind(*args, **{k: placeholder for k in r["kwargs"]})
+
+
+def test_register_with_the_reference_emsim_config():
+    """config.register on the reference's own emsim.config module (where its source tree
+    is given by EMSIM_REFERENCE_ROOT): set_backend("gb300") makes emsim's front-end
+    resolve the GB300 classes, and the reference's own names keep working."""
+    from oracle import ref_numpy
+    if not ref_numpy.available():
+        pytest.skip("reference source tree not available (EMSIM_REFERENCE_ROOT)")
+    from emsim_gb300 import backend
+    em = ref_numpy.load()
+    config.register(em)
+    try:
+        em.config.set_backend("gb300")
+        cur = em.config.get_current_backend()
+        assert cur.one_slice_builder is backend.OneSliceBuilder
+        assert cur.multi_slices_builder is backend.MultiSlicesBuilder
+        assert cur.wave_propagator is backend.WavePropagator
+        # the front-end resolves the class at call time (wave.py:7-16)
+        calls = []
+        orig = backend.WavePropagator.__init__
+
+        def spy(self, *a, **k):
+            calls.append(a)
+            orig(self, *a, **k)
+
+        backend.WavePropagator.__init__ = spy
+        try:
+            with pytest.raises(Exception):  # no GPU here: the plan creation itself fails
+                em.wave.get_raw_wave_propagator(64, 0.5, 200.0)
+        finally:
+            backend.WavePropagator.__init__ = orig
+        assert calls == [(64, 64, 0.5, 0.5, 200.0)]
+    finally:
+        em.config.set_backend("numpy")
+    assert em.config.get_current_backend().wave_propagator.__module__.endswith("wave_propagator_numpy")
