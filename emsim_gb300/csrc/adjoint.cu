@@ -210,6 +210,7 @@ int emsim_gb300_multislice_image_adjoint(emsim_gb300_wave_plan* p, const float* 
     cb.p2 = p2b;
     rb.slice_img_stride = slices_stride;
     rb.sigma = -p->sigma;  // conj(t_s)
+    rb.sigma_pi = -p->sigma_pi;
     rb.sigma_grad = p->sigma;
     rb.phi_img_stride = npix;
     const bool reduce = slices_stride == 0 && nb > 1;

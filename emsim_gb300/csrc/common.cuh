@@ -88,4 +88,14 @@ __device__ __forceinline__ float freq_sq_ref(int k1, int k2, float dfx, float df
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Transmission factor exp(i sigma V) as (cos, sin)(pi x) with x = (sigma / pi) V: the
+// argument is scaled once by the FP64-derived sigma / pi, and sincospif needs no large-
+// argument range reduction (CUDA's sincosf carries one), which keeps the fused passes'
+// code small.
+__device__ __forceinline__ float2 transmit_factor(float sigma_pi, float v) {
+    float s, c;
+    sincospif(sigma_pi * v, &s, &c);
+    return make_float2(c, s);
+}
+
 }  // namespace emsim_gb300

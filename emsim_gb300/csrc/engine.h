@@ -37,6 +37,7 @@ struct RowArgs {
     const float* slice = nullptr;  // (n1, n2) float32 per image
     long long slice_img_stride = 0;
     float sigma = 0.f;
+    float sigma_pi = 0.f;  // sigma / pi (FP64-derived): the transmit's sincospif argument scale
     float2 const_val = {0.f, 0.f};
     float2* phi = nullptr;  // ROW_STORE_PHI output / ROW_GRAD input, (n1, n2) per image
     long long phi_img_stride = 0;
@@ -179,7 +180,7 @@ cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, 
 }
 
 // element-wise kernels (any size)
-int ew_transmit(const float2* in, const float* slice, float2* out, long long n, float sigma, int n_img,
+int ew_transmit(const float2* in, const float* slice, float2* out, long long n, float sigma_pi, int n_img,
                 long long in_stride, long long slice_stride, long long out_stride, cudaStream_t st);
 int ew_fill(float2* out, long long n, float2 value, cudaStream_t st);
 int ew_intensity(const float2* in, float* out, long long n, cudaStream_t st);

@@ -154,7 +154,9 @@ __device__ __forceinline__ void seq_sync(int b) {
 // the 16 / R butterflies j = t + q T, whose inputs are its own positions; outputs go to
 // shared memory, or stay in registers (slot q + r 16 / R holds position j + r Ns) when
 // LAST.
-template <int L, int R, bool INV, bool LAST, bool TW_SMEM, class AddrF>
+// tw: a table of TWN entries exp(-2 pi i m / TWN) (the device table, TWN = TW_SIZE, or a
+// copy of its every (TW_SIZE / L)-th entry, TWN = L, e.g. staged in shared memory).
+template <int L, int R, bool INV, bool LAST, bool TW_SMEM, int TWN, class AddrF>
 __device__ __forceinline__ void pass(float2 (&v)[16], int Ns, float2* __restrict__ sm, int b, int t, AddrF addr,
                                      const float2* __restrict__ tw) {
     constexpr int T = L / 16;
@@ -167,7 +169,7 @@ __device__ __forceinline__ void pass(float2 (&v)[16], int Ns, float2* __restrict
 #pragma unroll
         for (int r = 0; r < R; ++r) x[r] = v[q + r * Q];
         if (Ns > 1) {
-            const int stride = fft::TW_SIZE / (Ns * R);
+            const int stride = TWN / (Ns * R);
             const float2 w1 = fft::twiddle<INV, TW_SMEM>(tw, k * stride);
             if (R == 16) {
                 // W^k and W^(8k) from the table, the other powers as running products
@@ -216,7 +218,7 @@ __device__ __forceinline__ void pass(float2 (&v)[16], int Ns, float2* __restrict
 // x[t + m L / 16] on entry and X[t + m L / 16] on return.  Every thread of the sequence
 // (of the CTA for SYNC_CTA) calls it; the exchange slots are free on entry and on return.
 // Unnormalised both ways.
-template <int L, bool INV, int SYNC, bool TW_SMEM = false, class AddrF>
+template <int L, bool INV, int SYNC, bool TW_SMEM = false, int TWN = fft::TW_SIZE, class AddrF>
 __device__ __forceinline__ void fft16n(float2 (&v)[16], float2* __restrict__ sm, int b, int t, AddrF addr,
                                        const float2* __restrict__ tw) {
     using S = Shape<L>;
@@ -231,15 +233,15 @@ __device__ __forceinline__ void fft16n(float2 (&v)[16], float2* __restrict__ sm,
         }
         const bool last = (p == S::NPASS - 1);
         if (p < S::P16) {
-            if (last) pass<L, 16, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
-            else pass<L, 16, INV, false, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+            if (last) pass<L, 16, INV, true, TW_SMEM, TWN>(v, Ns, sm, b, t, addr, tw);
+            else pass<L, 16, INV, false, TW_SMEM, TWN>(v, Ns, sm, b, t, addr, tw);
             Ns *= 16;
         } else if (S::REM == 3) {
-            pass<L, 8, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+            pass<L, 8, INV, true, TW_SMEM, TWN>(v, Ns, sm, b, t, addr, tw);
         } else if (S::REM == 2) {
-            pass<L, 4, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+            pass<L, 4, INV, true, TW_SMEM, TWN>(v, Ns, sm, b, t, addr, tw);
         } else {
-            pass<L, 2, INV, true, TW_SMEM>(v, Ns, sm, b, t, addr, tw);
+            pass<L, 2, INV, true, TW_SMEM, TWN>(v, Ns, sm, b, t, addr, tw);
         }
         if (!last) seq_sync<SYNC, S::T>(b);
     }

@@ -253,9 +253,7 @@ __global__ void __launch_bounds__(THREADS, 6) row_bf16_kernel(RowArgs a, int n_t
         // transform's stage-A row (r, n1) with n1 = k2, n2 = k1
 #pragma unroll
         for (int k1 = 0; k1 < NS; ++k1) {
-            float sn, cs;
-            sincosf(a.sigma * pot[k1], &sn, &cs);
-            const float2 t = cmul(make_float2(d[2 * k1], -d[2 * k1 + 1]), make_float2(cs, sn));
+            const float2 t = cmul(make_float2(d[2 * k1], -d[2 * k1 + 1]), transmit_factor(a.sigma_pi, pot[k1]));
             d[2 * k1] = t.x;
             d[2 * k1 + 1] = t.y;
         }

@@ -337,20 +337,17 @@ int generic_dft_cols(float2* data, int n_rows, int n_cols, bool inverse, const f
 // element-wise kernels
 // ---------------------------------------------------------------------------------
 __global__ void transmit_kernel(const float2* in, const float* __restrict__ slice, float2* out, long long n,
-                                float sigma, long long in_stride, long long slice_stride, long long out_stride) {
+                                float sigma_pi, long long in_stride, long long slice_stride, long long out_stride) {
     const long long img = blockIdx.y;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        float s, c;
-        sincosf(sigma * slice[img * slice_stride + i], &s, &c);
-        out[img * out_stride + i] = cmul(in[img * in_stride + i], make_float2(c, s));
-    }
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[img * out_stride + i] = cmul(in[img * in_stride + i], transmit_factor(sigma_pi, slice[img * slice_stride + i]));
 }
 
-int ew_transmit(const float2* in, const float* slice, float2* out, long long n, float sigma, int n_img,
+int ew_transmit(const float2* in, const float* slice, float2* out, long long n, float sigma_pi, int n_img,
                 long long in_stride, long long slice_stride, long long out_stride, cudaStream_t st) {
     int blocks = ceil_div(n, 256);
     if (blocks > 4096) blocks = 4096;
-    transmit_kernel<<<dim3(blocks, n_img), 256, 0, st>>>(in, slice, out, n, sigma, in_stride, slice_stride,
+    transmit_kernel<<<dim3(blocks, n_img), 256, 0, st>>>(in, slice, out, n, sigma_pi, in_stride, slice_stride,
                                                          out_stride);
     EMSIM_CHECK_LAUNCH();
     return EMSIM_GB300_OK;

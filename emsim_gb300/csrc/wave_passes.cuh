@@ -69,11 +69,7 @@ __global__ void __launch_bounds__(512) row_pass_kernel(RowArgs a) {
     if (OPS & ROW_TRANSMIT) {
         const float* vs = a.slice + img * a.slice_img_stride + (long long)row * N;
 #pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            float s, c;
-            sincosf(a.sigma * __ldg(vs + t + m * T), &s, &c);
-            v[m] = cmul(v[m], make_float2(c, s));
-        }
+        for (int m = 0; m < 8; ++m) v[m] = cmul(v[m], transmit_factor(a.sigma_pi, __ldg(vs + t + m * T)));
     }
 
     if (OPS & ROW_STORE_PHI) {

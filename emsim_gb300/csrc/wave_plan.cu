@@ -128,6 +128,7 @@ RowArgs base_row(const emsim_gb300_wave_plan* p) {
     a.out_img_stride = npix;
     a.out_int_img_stride = npix;
     a.sigma = p->sigma;
+    a.sigma_pi = p->sigma_pi;
     a.n_rows = p->n1;
     return a;
 }
@@ -208,6 +209,7 @@ int emsim_gb300_wave_plan_create(int n1, int n2, double d1, double d2, double wa
     p->wave_length = wave_length;
     p->gamma = relativity_gamma;
     p->sigma = (float)(wave_length * relativity_gamma);
+    p->sigma_pi = (float)(wave_length * relativity_gamma / M_PI);
     const float d1f = (float)d1, d2f = (float)d2;
     p->dfx = 1.0f / d1f / (float)n1;
     p->dfy = 1.0f / d2f / (float)n2;
@@ -283,7 +285,7 @@ int emsim_gb300_slice_transmit(emsim_gb300_wave_plan* p, const void* wave, const
     EMSIM_TRY(check_device(p));
     EMSIM_REQUIRE(wave && slice && wave_out && nb >= 1, EMSIM_GB300_ERR_INVALID, "slice_transmit: bad arguments");
     const long long npix = (long long)p->n1 * p->n2;
-    return ew_transmit((const float2*)wave, slice, (float2*)wave_out, npix, p->sigma, nb, npix, slice_stride, npix,
+    return ew_transmit((const float2*)wave, slice, (float2*)wave_out, npix, p->sigma_pi, nb, npix, slice_stride, npix,
                        (cudaStream_t)stream);
 }
 
@@ -318,7 +320,7 @@ int emsim_gb300_singleslice_propagate(emsim_gb300_wave_plan* p, const void* wave
     float2* out = (float2*)wave_out;
     const long long npix = (long long)p->n1 * p->n2;
     if (!p->fast) {
-        EMSIM_TRY(ew_transmit((const float2*)wave, slice, out, npix, p->sigma, nb, npix, slice_stride, npix, st));
+        EMSIM_TRY(ew_transmit((const float2*)wave, slice, out, npix, p->sigma_pi, nb, npix, slice_stride, npix, st));
         return g_space(p, out, out, dz, nb, st);
     }
     const float4* p1;
@@ -395,7 +397,7 @@ int emsim_gb300_multislice_propagate(emsim_gb300_wave_plan* p, const void* wave,
     if (!p->fast) {
         const float2* cur = (const float2*)wave;
         for (int s = 0; s < n_slices; ++s) {
-            EMSIM_TRY(ew_transmit(cur, slices + (long long)s * npix, out, npix, p->sigma, nb, npix, slices_stride,
+            EMSIM_TRY(ew_transmit(cur, slices + (long long)s * npix, out, npix, p->sigma_pi, nb, npix, slices_stride,
                                   npix, st));
             EMSIM_TRY(g_space(p, out, out, dz, nb, st));
             cur = out;

@@ -17,6 +17,7 @@ struct emsim_gb300_wave_plan {
     double d1 = 0, d2 = 0;
     double wave_length = 0, gamma = 0;
     float sigma = 0.f;           // gamma * lambda formed in FP64, rounded once
+    float sigma_pi = 0.f;        // gamma * lambda / pi formed in FP64, rounded once
     float dfx = 0.f, dfy = 0.f;  // 1.0f / d / n in float32 (WavePropagator.cpp:19-20)
     double dfx64 = 0, dfy64 = 0;
     float filter2 = 0.f;  // (0.6667f * 0.5f / max(d1, d2))^2 in float32 (WavePropagator.cpp:21-23)

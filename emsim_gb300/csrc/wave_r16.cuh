@@ -42,6 +42,22 @@ __device__ __forceinline__ void fft_line(float2 (&v)[16], float2* __restrict__ s
     else fft16::fft16n<L, INV, SYNC>(v, sm, b, t, addr, tw);
 }
 
+// The column pass's transforms read the twiddles of their length from a copy in shared
+// memory (every (4096 / L)-th entry of the device table, staged once per CTA), which
+// spares the persistent CTA a global load at the start of every butterfly group.
+template <int L, bool INV>
+__device__ __forceinline__ void fft_col(float2 (&v)[16], float2* __restrict__ sm, int b, int t,
+                                        const fft16::ColSlot& addr, const float2* __restrict__ tw,
+                                        const float2* __restrict__ s_tw) {
+    if constexpr (L == 256) fft16::fft256<INV, false>(v, sm, b, t, addr, tw);
+    else if constexpr (L > 2048) fft16::fft16n<L, INV, fft16::SYNC_CTA>(v, sm, b, t, addr, tw);
+    else fft16::fft16n<L, INV, fft16::SYNC_CTA, true, L>(v, sm, b, t, addr, s_tw);
+}
+
+// (lengths 512..2048: at 4096 the two stages and the row factors already take 192 KB)
+template <int L>
+constexpr int col_tw_entries() { return L == 256 || L > 2048 ? 0 : L; }
+
 template <int L, int OPS>
 __global__ void __launch_bounds__(256, 2) row16_kernel(RowArgs a, int B, int tiles_per_img, int n_tiles) {
     constexpr int T = RowCfg<L>::T;
@@ -115,11 +131,7 @@ __global__ void __launch_bounds__(256, 2) row16_kernel(RowArgs a, int B, int til
         if (OPS & ROW_IFFT) fft_line<L, true, SYNC>(v, stage, b, t, addr, a.tw);
         if (OPS & ROW_TRANSMIT) {
 #pragma unroll
-            for (int m = 0; m < 16; ++m) {
-                float s, c;
-                sincosf(a.sigma * vs[m], &s, &c);
-                v[m] = cmul(v[m], make_float2(c, s));
-            }
+            for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], transmit_factor(a.sigma_pi, vs[m]));
         }
         if (OPS & ROW_FFT) fft_line<L, false, SYNC>(v, stage, b, t, addr, a.tw);
 
@@ -159,6 +171,8 @@ __global__ void __launch_bounds__(512, 1)
     float4* s_p1 = reinterpret_cast<float4*>(bar + 2);
     if (MODE == COL_PROPAGATE)
         for (int i = threadIdx.x; i < L; i += blockDim.x) s_p1[i] = __ldg(a.p1 + i);
+    float2* s_tw = reinterpret_cast<float2*>(s_p1 + L);
+    for (int i = threadIdx.x; i < col_tw_entries<L>(); i += blockDim.x) s_tw[i] = __ldg(a.tw + i * (fft::TW_SIZE / L));
     const fft16::ColSlot addr{B, B >= 16 ? 0 : (16 / B) - 1};
     const int live_per_img = lt_lo + lt_hi;
     const int n_tiles = live_per_img * n_img;
@@ -209,7 +223,7 @@ __global__ void __launch_bounds__(512, 1)
         int img, ct;
         locate(tile, img, ct);
         const int col = ct * B + b;
-        if (MODE != COL_INV) fft_line<L, false, fft16::SYNC_CTA>(v, stage, b, t, addr, a.tw);
+        if (MODE != COL_INV) fft_col<L, false>(v, stage, b, t, addr, a.tw, s_tw);
         if (MODE == COL_PROPAGATE) {
             const int k2a = abs(fftfreq_int(col, a.n_cols));
             const float2 p2 = __ldg(a.p2 + col);
@@ -227,7 +241,7 @@ __global__ void __launch_bounds__(512, 1)
             for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], lens_factor(fftfreq_int(t + m * T, L), k2, fy * fy, c2, a));
         }
         if (MODE == COL_PROPAGATE || MODE == COL_LENS || MODE == COL_INV)
-            fft_line<L, true, fft16::SYNC_CTA>(v, stage, b, t, addr, a.tw);
+            fft_col<L, true>(v, stage, b, t, addr, a.tw, s_tw);
 
         float2* base = a.data + img * a.img_stride + col;
 #pragma unroll
@@ -306,7 +320,8 @@ bool launch_col16_n(int mode, const ColArgs& a, int n_img, cudaStream_t st, int*
     const int threads = B * C::T;
     const int tiles_per_img = a.n_cols / B;
     const LiveTiles lt = mode == COL_PROPAGATE ? live_tiles(a, B, tiles_per_img) : LiveTiles{tiles_per_img, 0};
-    const size_t smem = 2 * (size_t)L * B * sizeof(float2) + 2 * sizeof(uint64_t) + L * sizeof(float4);
+    const size_t smem = 2 * (size_t)L * B * sizeof(float2) + 2 * sizeof(uint64_t) + L * sizeof(float4) +
+                        r16::col_tw_entries<L>() * sizeof(float2);
     CUtensorMap map;
     *status = make_col_tensor_map(&map, a.data, (long long)n_img * L, a.n_cols, B, C::BOXR);
     if (*status != EMSIM_GB300_OK) return true;

@@ -115,11 +115,7 @@ __global__ void __launch_bounds__(RowTma<N>::THREADS, RowTma<N>::MIN_BLOCKS)
         }
         if (OPS & ROW_TRANSMIT) {
 #pragma unroll
-            for (int m = 0; m < 8; ++m) {
-                float s, c;
-                sincosf(a.sigma * vs[m], &s, &c);
-                v[m] = cmul(v[m], make_float2(c, s));
-            }
+            for (int m = 0; m < 8; ++m) v[m] = cmul(v[m], transmit_factor(a.sigma_pi, vs[m]));
         }
         if (OPS & ROW_STORE_PHI) {
             float2* ph = a.phi + img * a.phi_img_stride + row * N;
