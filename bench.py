@@ -643,6 +643,10 @@ def run_ours(args):
     rl_build = build_roofline(torch, db, peak, flush=flush)
     t_steps = rl_step["step_s"] * db.ns
     traffic = read_traffic()
+    # the captured figures hold for the batch they were captured on (null for another)
+    for key in ("slice_step_2048", "slice_build_2048"):
+        if traffic.get(key + "_images") != db.B:
+            traffic.pop(key, None)
     if t_steps >= rl_build["seconds"]:
         roofline = {"bound": "hbm", "kernel": "slice step = fused row pass + column pass (2048^2, %d images), "
                                               "averaged over the 400 steps of the headline step" % db.B,
