@@ -1,7 +1,8 @@
 """Image formation straight from atoms with the slices built chunk by chunk
 (emsim_gb300_image_from_atoms_z): bitwise equal to the slice build followed by the fused
 image for every chunk size, including an odd slice count (a half-empty last pair) and a
-chunk size that does not divide the pair count; and the Pipe route that uses it for
+chunk size that does not divide the pair count, with the per-tile (128^2, 256^2) and the
+persistent (512^2) slice column pass; and the Pipe route that uses it for
 large stacks against the FP64 oracle.
 """
 import numpy as np
@@ -39,7 +40,7 @@ def _device_batch(backend, mols):
     return xyz, z, off, shift
 
 
-@pytest.mark.parametrize("n,ns", [(128, 9), (256, 12)])
+@pytest.mark.parametrize("n,ns", [(128, 9), (256, 12), (512, 7)])
 def test_chunked_image_bitwise_equal(eng, n, ns):
     backend = eng
     mols = [om.protein_blob(3000 + 500 * k, radius=18.0, seed=40 + k) for k in range(3)]
