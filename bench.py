@@ -487,6 +487,36 @@ def plain_cufft_extra(torch, db: DeviceImages, flush, reps: int = 3) -> dict:
             "speedup": round(t_plain / t_fused, 3), "rel_l2_plain_vs_fused": rel}
 
 
+def graphs_extra(torch, n_mols: int = 4, reps: int = 20) -> dict:
+    """Small batches through Pipe.run_batch(to_host=True), where launching is a large part
+    of a call: n_mols blobs of the blob workload per call, eager launches against the
+    CUDA graph that Pipe(cuda_graphs=True) replays for a structure seen before (both warm,
+    wall clock per call, images checked bitwise equal)."""
+    import time
+    from emsim_gb300 import atoms, pipe, tem
+    from emsim_gb300.synth import protein_blob
+    W = BLOB
+    mols = [atoms.AtomList(*protein_blob(W["n_atoms"], W["radius"], 500 + s)) for s in range(n_mols)]
+    t_ = tem.TEM(electron_dose=W["dose"], beam_energy_kev=W["kev"], cs_mm=W["cs_mm"], defocus=W["defocus"],
+                 aperture=W["aperture"])
+    out = {"workload": f"{n_mols} blobs of the blob workload per Pipe.run_batch(to_host=True) call "
+                       f"(roi {W['roi']}, 40 slices), wall clock per call"}
+    imgs = {}
+    for mode in ("eager", "cuda_graphs"):
+        p = pipe.Pipe(t_, resolution=W["resolution"], slice_thickness=W["slice_thickness"], roi=W["roi"],
+                      add_water=False, cuda_graphs=(mode == "cuda_graphs"))
+        for _ in range(3):
+            imgs[mode] = p.run_batch(mols, to_host=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            p.run_batch(mols, to_host=True)
+        dt = (time.perf_counter() - t0) / reps
+        out[mode] = {"images_per_s": round(n_mols / dt, 1), "ms_per_call": round(1e3 * dt, 3)}
+    out["bitwise_equal"] = all(bool(np.array_equal(a, b)) for a, b in zip(imgs["eager"], imgs["cuda_graphs"]))
+    return out
+
+
 def batching_extra(torch, p, n_blobs: int = 256, reps: int = 2) -> dict:
     """The batching workload through Pipe.run_batch: 256 blobs with log-uniform 5k-200k
     atoms at 0.1 A^-3, random orientations, roi 256 or 512, every other one in amorphous
@@ -680,6 +710,7 @@ def run_ours(args):
     del bdb
     torch.cuda.empty_cache()
     diff = differentiation_extra(torch)
+    graphs = graphs_extra(torch)
     batching = batching_extra(torch, pipe.Pipe(
         tem.TEM(electron_dose=BLOB["dose"], beam_energy_kev=BLOB["kev"], cs_mm=BLOB["cs_mm"],
                 defocus=BLOB["defocus"], aperture=BLOB["aperture"]),
@@ -714,6 +745,7 @@ def run_ours(args):
         "chunked_slices": chunked,
         "differentiation": diff,
         "batching": batching,
+        "api_cuda_graphs": graphs,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -62,6 +62,23 @@ def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
     return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
 
 
+class Prepared:
+    """Device work whose metadata already sits on the device and whose buffers are
+    allocated: calling it makes only native calls on the current stream (no allocation,
+    no host-to-device copy, no synchronisation), so it can be captured in a CUDA graph
+    and replayed.  ``result`` is the tensor it writes; ``keep`` holds what the calls
+    read (device metadata, workspaces, host scalars' arrays)."""
+
+    __slots__ = ("_fn", "result", "_keep")
+
+    def __init__(self, fn, result: torch.Tensor, keep=()):
+        self._fn, self.result, self._keep = fn, result, keep
+
+    def __call__(self) -> torch.Tensor:
+        self._fn()
+        return self.result
+
+
 def as_device(x, dtype: torch.dtype) -> torch.Tensor:
     """Contiguous tensor of ``dtype`` on the current CUDA device (copy only if needed)."""
     dev = _device()
@@ -225,28 +242,28 @@ class MultiSlicesBuilder:
                                   symmetric_bandlimit)[0]
 
 
-def build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tensor, z: torch.Tensor,
-                                   offsets: torch.Tensor, shift: torch.Tensor, mol_index: Sequence[int], n_mol: int,
-                                   symmetric_bandlimit: bool = True,
-                                   slot_slices: Optional[Sequence[int]] = None) -> DeviceArray:
-    """Slices of molecules ``mol_index`` of a device-resident batch: ``xyz`` (n_atoms, 3)
-    float32, ``z`` (n_atoms) int32, ``offsets`` (n_mol + 1) uint32 atom offsets, ``shift``
-    (n_mol, 3) float32 per-molecule translation (centralisation).  Returns
-    (len(mol_index), n_slices, n1, n2) float32.  ``slot_slices``: each molecule's own slice
-    count (<= builder.n_slice; ragged batch): molecule k is binned on the slice axis of
-    its own count and fills slices [0, slot_slices[k]) of its stack."""
+def _element_slots(builder: MultiSlicesBuilder) -> np.ndarray:
+    eoz = np.full(128, -1, dtype=np.int32)
+    for k, zz in enumerate(sorted(int(v) for v in builder.unique_elements)):
+        if 0 <= zz < 128:
+            eoz[zz] = k
+    return eoz
+
+
+def prepare_build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tensor, z: torch.Tensor,
+                                           offsets: torch.Tensor, shift: torch.Tensor, mol_index: Sequence[int],
+                                           n_mol: int, symmetric_bandlimit: bool = True,
+                                           slot_slices: Optional[Sequence[int]] = None) -> Prepared:
+    """:func:`build_slices_from_device_atoms` with its metadata uploaded and its output and
+    workspace allocated; calling the result runs the build."""
     plan = builder._plan if symmetric_bandlimit else slice_plan(
         builder.unique_elements, builder.n_slice, builder.n1, builder.n2, builder.dz, builder.d1, builder.d2,
         False)[0]
     dev = _device()
     slot = np.full(n_mol, -1, dtype=np.int32)
     slot[list(mol_index)] = np.arange(len(mol_index), dtype=np.int32)
-    eoz = np.full(128, -1, dtype=np.int32)
-    for k, zz in enumerate(sorted(int(v) for v in builder.unique_elements)):
-        if 0 <= zz < 128:
-            eoz[zz] = k
     nb = len(mol_index)
-    parts = [slot, eoz]
+    parts = [slot, _element_slots(builder)]
     if slot_slices is not None:
         ss = np.asarray(slot_slices, dtype=np.int32).reshape(-1)
         if ss.shape[0] != nb or ss.min(initial=1) < 1 or ss.max(initial=1) > builder.n_slice:
@@ -258,14 +275,60 @@ def build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tenso
     nbytes = int(_native.load().emsim_gb300_build_slices_workspace_size(plan.handle, n_atoms, nb))
     ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
     eoz_ptr = ctypes.c_void_p(meta.data_ptr() + 4 * n_mol)
-    if slot_slices is None:
-        _native.call("emsim_gb300_build_slices_z", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets), n_mol,
-                     _ptr(shift), _ptr(meta), eoz_ptr, nb, _ptr(out), _ptr(ws), nbytes, _stream())
-    else:
-        _native.call("emsim_gb300_build_slices_ragged", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets),
-                     n_mol, _ptr(shift), _ptr(meta), eoz_ptr, ctypes.c_void_p(meta.data_ptr() + 4 * (n_mol + 128)),
-                     nb, _ptr(out), _ptr(ws), nbytes, _stream())
-    return _wrap(out)
+
+    def run():
+        if slot_slices is None:
+            _native.call("emsim_gb300_build_slices_z", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets),
+                         n_mol, _ptr(shift), _ptr(meta), eoz_ptr, nb, _ptr(out), _ptr(ws), nbytes, _stream())
+        else:
+            _native.call("emsim_gb300_build_slices_ragged", plan.handle, _ptr(xyz), _ptr(z), n_atoms, _ptr(offsets),
+                         n_mol, _ptr(shift), _ptr(meta), eoz_ptr,
+                         ctypes.c_void_p(meta.data_ptr() + 4 * (n_mol + 128)), nb, _ptr(out), _ptr(ws), nbytes,
+                         _stream())
+
+    return Prepared(run, out, (plan, meta, ws, xyz, z, offsets, shift))
+
+
+def build_slices_from_device_atoms(builder: MultiSlicesBuilder, xyz: torch.Tensor, z: torch.Tensor,
+                                   offsets: torch.Tensor, shift: torch.Tensor, mol_index: Sequence[int], n_mol: int,
+                                   symmetric_bandlimit: bool = True,
+                                   slot_slices: Optional[Sequence[int]] = None) -> DeviceArray:
+    """Slices of molecules ``mol_index`` of a device-resident batch: ``xyz`` (n_atoms, 3)
+    float32, ``z`` (n_atoms) int32, ``offsets`` (n_mol + 1) uint32 atom offsets, ``shift``
+    (n_mol, 3) float32 per-molecule translation (centralisation).  Returns
+    (len(mol_index), n_slices, n1, n2) float32.  ``slot_slices``: each molecule's own slice
+    count (<= builder.n_slice; ragged batch): molecule k is binned on the slice axis of
+    its own count and fills slices [0, slot_slices[k]) of its stack."""
+    return _wrap(prepare_build_slices_from_device_atoms(builder, xyz, z, offsets, shift, mol_index, n_mol,
+                                                        symmetric_bandlimit, slot_slices)())
+
+
+def prepare_image_from_device_atoms(builder: MultiSlicesBuilder, wp: "WavePropagator", xyz: torch.Tensor,
+                                    z: torch.Tensor, offsets: torch.Tensor, shift: torch.Tensor,
+                                    mol_index: Sequence[int], n_mol: int, electron_dose: float, cs_mm: float, defocus,
+                                    aperture: float, chunk_pairs: int = 0) -> Prepared:
+    """:func:`image_from_device_atoms` with its metadata uploaded and its image and
+    workspace allocated; calling the result forms the images."""
+    plan = builder._plan
+    dev = _device()
+    slot = np.full(n_mol, -1, dtype=np.int32)
+    slot[list(mol_index)] = np.arange(len(mol_index), dtype=np.int32)
+    nb = len(mol_index)
+    meta = torch.from_numpy(np.concatenate([slot, _element_slots(builder)])).to(dev, non_blocking=True)
+    n_atoms = int(xyz.shape[0])
+    lib = _native.load()
+    nbytes = int(lib.emsim_gb300_image_from_atoms_workspace_size(plan.handle, n_atoms, nb, int(chunk_pairs)))
+    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+    img = torch.empty((nb, builder.n1, builder.n2), dtype=torch.float32, device=dev)
+    dfs = np.ascontiguousarray(np.atleast_1d(np.asarray(defocus, dtype=np.float64)))
+
+    def run():
+        _native.call("emsim_gb300_image_from_atoms_z", plan.handle, wp._plan.handle, _ptr(xyz), _ptr(z), n_atoms,
+                     _ptr(offsets), n_mol, _ptr(shift), _ptr(meta), ctypes.c_void_p(meta.data_ptr() + 4 * n_mol), nb,
+                     float(electron_dose), float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                     len(dfs), float(aperture), _ptr(img), int(chunk_pairs), _ptr(ws), nbytes, _stream())
+
+    return Prepared(run, img, (plan, wp, meta, ws, dfs, xyz, z, offsets, shift))
 
 
 def image_from_device_atoms(builder: MultiSlicesBuilder, wp: "WavePropagator", xyz: torch.Tensor, z: torch.Tensor,
@@ -277,27 +340,8 @@ def image_from_device_atoms(builder: MultiSlicesBuilder, wp: "WavePropagator", x
     pairs at a time (``emsim_gb300_image_from_atoms_z``): the slice stack is never held
     whole, and the images are bitwise those of build_slices_from_device_atoms followed
     by ``WavePropagator.image``.  Returns (len(mol_index), n1, n2) float32."""
-    plan = builder._plan
-    dev = _device()
-    slot = np.full(n_mol, -1, dtype=np.int32)
-    slot[list(mol_index)] = np.arange(len(mol_index), dtype=np.int32)
-    eoz = np.full(128, -1, dtype=np.int32)
-    for k, zz in enumerate(sorted(int(v) for v in builder.unique_elements)):
-        if 0 <= zz < 128:
-            eoz[zz] = k
-    nb = len(mol_index)
-    meta = torch.from_numpy(np.concatenate([slot, eoz])).to(dev, non_blocking=True)
-    n_atoms = int(xyz.shape[0])
-    lib = _native.load()
-    nbytes = int(lib.emsim_gb300_image_from_atoms_workspace_size(plan.handle, n_atoms, nb, int(chunk_pairs)))
-    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
-    img = torch.empty((nb, builder.n1, builder.n2), dtype=torch.float32, device=dev)
-    dfs = np.atleast_1d(np.asarray(defocus, dtype=np.float64))
-    _native.call("emsim_gb300_image_from_atoms_z", plan.handle, wp._plan.handle, _ptr(xyz), _ptr(z), n_atoms,
-                 _ptr(offsets), n_mol, _ptr(shift), _ptr(meta), ctypes.c_void_p(meta.data_ptr() + 4 * n_mol), nb,
-                 float(electron_dose), float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(dfs),
-                 float(aperture), _ptr(img), int(chunk_pairs), _ptr(ws), nbytes, _stream())
-    return _wrap(img)
+    return _wrap(prepare_image_from_device_atoms(builder, wp, xyz, z, offsets, shift, mol_index, n_mol,
+                                                 electron_dose, cs_mm, defocus, aperture, chunk_pairs)())
 
 
 def build_slices_batch(builder: MultiSlicesBuilder, mols, symmetric_bandlimit: bool = True) -> DeviceArray:
@@ -472,26 +516,39 @@ class WavePropagator:
         ``slices``: (n_slices, n1, n2) shared or (B, n_slices, n1, n2); ``defocus``: a
         number or a sequence (image b uses defocus[b % len]).  Returns (n1, n2) or
         (B, n1, n2) float32 intensities (and the exit waves when requested)."""
-        n1, n2 = self.wave_shape
         s = as_device(slices, torch.float32)
+        prep = self.prepare_image(s, dz, electron_dose, cs_mm, defocus, aperture, n_batch, return_exit_wave)
+        img = prep()
+        squeeze = s.dim() == 3 and n_batch is None and not np.ndim(defocus)
+        out = _wrap(img[0] if squeeze else img)
+        if return_exit_wave:
+            ew = prep._keep[-1]
+            return out, _wrap(ew[0] if squeeze else ew)
+        return out
+
+    def prepare_image(self, slices: torch.Tensor, dz: float, electron_dose: float, cs_mm: float, defocus,
+                      aperture: float, n_batch: Optional[int] = None, return_exit_wave: bool = False) -> Prepared:
+        """:meth:`image` on device slices with its buffers allocated; calling the result
+        forms the (B, n1, n2) images (the exit waves, when requested, in ``_keep[-1]``)."""
+        n1, n2 = self.wave_shape
+        s = slices
         if s.dim() == 4:
             nb, ns, sstride = int(s.shape[0]), int(s.shape[1]), int(s.shape[1]) * n1 * n2
         else:
             ns, sstride = int(s.shape[0]), 0
             nb = n_batch or (len(defocus) if np.ndim(defocus) else 1)
-        dfs = np.atleast_1d(np.asarray(defocus, dtype=np.float64))
+        dfs = np.ascontiguousarray(np.atleast_1d(np.asarray(defocus, dtype=np.float64)))
         dev = _device()
         img = torch.empty((nb, n1, n2), dtype=torch.float32, device=dev)
         work = torch.empty((nb, n1, n2), dtype=torch.complex64, device=dev)
         ew = torch.empty_like(work) if return_exit_wave else None
-        _native.call("emsim_gb300_multislice_image", self._plan.handle, _ptr(s), ns, sstride, float(dz),
-                     float(electron_dose), float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                     len(dfs), float(aperture), _ptr(img), _ptr(work), _ptr(ew), nb, _stream())
-        squeeze = s.dim() == 3 and n_batch is None and not np.ndim(defocus)
-        img = _wrap(img[0] if squeeze else img)
-        if return_exit_wave:
-            return img, _wrap(ew[0] if squeeze else ew)
-        return img
+
+        def run():
+            _native.call("emsim_gb300_multislice_image", self._plan.handle, _ptr(s), ns, sstride, float(dz),
+                         float(electron_dose), float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                         len(dfs), float(aperture), _ptr(img), _ptr(work), _ptr(ew), nb, _stream())
+
+        return Prepared(run, img, (self._plan, s, dfs, work, ew))
 
 
 def focal_spread_quadrature(defocus: float, focal_spread: float, n: int = 7) -> Tuple[np.ndarray, np.ndarray]:
@@ -506,6 +563,30 @@ def focal_spread_quadrature(defocus: float, focal_spread: float, n: int = 7) -> 
     return float(defocus) + math.sqrt(2.0) * float(focal_spread) * x, w / math.sqrt(math.pi)
 
 
+def prepare_image_ragged(wp: "WavePropagator", stacks: torch.Tensor, n_slices: Sequence[int], dz: float,
+                         electron_dose: float, cs_mm: float, defocus, aperture: float) -> Prepared:
+    """:func:`image_ragged` for device stacks already ordered longest first, with its
+    buffers allocated; calling the result forms the images (in the stacks' order)."""
+    s = stacks
+    nb, smax, n1, n2 = (int(x) for x in s.shape)
+    ns = np.ascontiguousarray(np.asarray(n_slices, dtype=np.int32).reshape(-1))
+    if ns.shape[0] != nb or ns.min(initial=1) < 1 or ns.max(initial=1) > smax:
+        raise ValueError(f"n_slices must hold {nb} counts in [1, {smax}]")
+    if np.any(np.diff(ns) > 0):
+        raise ValueError("prepare_image_ragged wants the stacks ordered by slice count, longest first")
+    dfs = np.ascontiguousarray(np.atleast_1d(np.asarray(defocus, dtype=np.float64)))
+    img = torch.empty((nb, n1, n2), dtype=torch.float32, device=s.device)
+    work = torch.empty((nb, n1, n2), dtype=torch.complex64, device=s.device)
+
+    def run():
+        _native.call("emsim_gb300_multislice_image_ragged", wp._plan.handle, _ptr(s), smax * n1 * n2,
+                     ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), float(dz), float(electron_dose),
+                     float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(dfs), float(aperture),
+                     _ptr(img), _ptr(work), nb, _stream())
+
+    return Prepared(run, img, (wp._plan, s, ns, dfs, work))
+
+
 def image_ragged(wp: "WavePropagator", stacks, n_slices: Sequence[int], dz: float, electron_dose: float,
                  cs_mm: float, defocus, aperture: float) -> DeviceArray:
     """Images of a ragged batch: ``stacks`` (B, S_max, n1, n2) float32 where image b uses
@@ -513,7 +594,7 @@ def image_ragged(wp: "WavePropagator", stacks, n_slices: Sequence[int], dz: floa
     over the images that still have a slice (``emsim_gb300_multislice_image_ragged``);
     results come back in input order, (B, n1, n2) float32."""
     s = as_device(stacks, torch.float32)
-    nb, smax, n1, n2 = (int(x) for x in s.shape)
+    nb, smax = int(s.shape[0]), int(s.shape[1])
     ns = np.asarray(n_slices, dtype=np.int32).reshape(-1)
     if ns.shape[0] != nb or ns.min(initial=1) < 1 or ns.max(initial=1) > smax:
         raise ValueError(f"n_slices must hold {nb} counts in [1, {smax}]")
@@ -523,13 +604,7 @@ def image_ragged(wp: "WavePropagator", stacks, n_slices: Sequence[int], dz: floa
     if np.any(order != np.arange(nb)):
         s = s[torch.as_tensor(order, device=dev)].contiguous()
         dfs = np.ascontiguousarray(np.resize(dfs, nb)[order]) if dfs.size > 1 else dfs
-    ns_sorted = np.ascontiguousarray(ns[order])
-    img = torch.empty((nb, n1, n2), dtype=torch.float32, device=dev)
-    work = torch.empty((nb, n1, n2), dtype=torch.complex64, device=dev)
-    _native.call("emsim_gb300_multislice_image_ragged", wp._plan.handle, _ptr(s), smax * n1 * n2,
-                 ns_sorted.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), float(dz), float(electron_dose),
-                 float(cs_mm), dfs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(dfs), float(aperture),
-                 _ptr(img), _ptr(work), nb, _stream())
+    img = prepare_image_ragged(wp, s, ns[order], dz, electron_dose, cs_mm, dfs, aperture)()
     if np.any(order != np.arange(nb)):
         inv = np.empty(nb, dtype=np.int64)
         inv[order] = np.arange(nb)

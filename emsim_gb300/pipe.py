@@ -4,7 +4,10 @@
 lateral size ``roi`` and thickness ``slice_thickness`` (optionally with voxel water),
 plane wave, multislice, objective lens, |psi|^2 - and forms the image in one fused
 engine call after the slices exist.  ``run_batch`` forms many images, one engine call
-per group of equal (n_slices, roi).
+per group of equal (n_slices, roi).  With ``cuda_graphs=True`` a batch whose structure
+(atom and molecule counts, stack shapes, elements, defocus values) was seen before
+replays one CUDA graph of its slice builds and image formation instead of launching
+them one by one.
 """
 from __future__ import annotations
 
@@ -42,11 +45,61 @@ def _fast_len(n: int) -> bool:
     return 8 <= n <= 4096 and (n & (n - 1)) == 0
 
 
+class _GraphCache:
+    """CUDA graphs of a Pipe's batches, per input-buffer set, keyed by batch structure.
+
+    A structure is captured the second time it is seen (the first run creates the plans
+    and tables the launches use, which allocates and so cannot be captured), replayed
+    from then on.  At most ``max_entries`` graphs are kept per buffer set (least recently
+    used dropped); a buffer set that grows drops all of its graphs, whose launches read
+    the old buffers."""
+
+    def __init__(self, max_entries: int = 2, max_seen: int = 4096):
+        self.max_entries = max_entries
+        self.max_seen = max_seen
+        self._entries = {}  # buf_key -> OrderedDict(key -> entry)
+        self._seen = {}
+
+    def get(self, buf_key, key):
+        ent = self._entries.get(buf_key)
+        if ent is None or key not in ent:
+            return None
+        ent.move_to_end(key)
+        return ent[key]
+
+    def sighting(self, buf_key, key) -> int:
+        """How many times (this one included) the structure was met on this buffer set."""
+        if len(self._seen) >= self.max_seen:
+            self._seen.clear()
+        n = self._seen.get((buf_key, key), 0) + 1
+        self._seen[(buf_key, key)] = n
+        return n
+
+    def put(self, buf_key, key, entry) -> None:
+        from collections import OrderedDict
+        ent = self._entries.setdefault(buf_key, OrderedDict())
+        ent[key] = entry
+        ent.move_to_end(key)
+        while len(ent) > self.max_entries:
+            ent.popitem(last=False)
+
+    def drop(self, buf_key) -> None:
+        self._entries.pop(buf_key, None)
+        for k in [k for k in self._seen if k[0] == buf_key]:
+            del self._seen[k]
+
+    def __len__(self) -> int:
+        return sum(len(v) for v in self._entries.values())
+
+
 class Pipe:
     def __init__(self, microscope: tem.TEM, resolution: float, slice_thickness: float,
                  roi: Optional[Union[int, Tuple[int, int]]] = None, n_slices: Optional[int] = None,
-                 add_water: bool = True, upto_exit_wave: bool = False):
+                 add_water: bool = True, upto_exit_wave: bool = False, cuda_graphs: bool = False):
         self._resolution = resolution
+        # run_batch / submit_batch replay a CUDA graph for a batch structure seen before
+        self.cuda_graphs = cuda_graphs
+        self._graphs = _GraphCache()
         self._pixel_size = 0.5 * resolution
         self.microscope = microscope
         self.slice_thickness = slice_thickness
@@ -168,7 +221,7 @@ class Pipe:
             return [im.get() for im in imgs] if to_host else imgs
         if to_host:
             return self.submit_batch(mols, defocus, rois).result()
-        done = self._queue_batch(mols, defocus, rois, torch.cuda.current_stream(), 0)
+        done = self._queue_batch(mols, defocus, rois, torch.cuda.current_stream(), "sync")
         out: List = [None] * len(mols)
         for idx, imgs in done:
             for j, i in enumerate(idx):
@@ -268,7 +321,7 @@ class Pipe:
                 streams.append(st)
             with torch.cuda.stream(st):
                 part = self._launch_chunk(mols[a:b], None if defocus is None else defocus[a:b],
-                                          None if rois is None else rois[a:b])
+                                          None if rois is None else rois[a:b], (slot, c))
                 for idx, imgs in part:
                     if st is not main:
                         imgs.record_stream(main)
@@ -286,7 +339,58 @@ class Pipe:
             pool[(dev, key)] = torch.cuda.Stream()
         return pool[(dev, key)]
 
-    def _launch_chunk(self, mols, defocus, rois):
+    def _inputs(self, buf_key, n_atoms: int, nm: int):
+        """Device input buffers of one buffer set (grown on demand), so that a replayed
+        graph finds the batch at the addresses it was captured with."""
+        bufs = getattr(self, "_in_bufs", None)
+        if bufs is None:
+            bufs = self._in_bufs = {}
+        dev = backend._device()
+        b = bufs.get(buf_key)
+        if b is None or b["xyz"].device != dev or b["xyz"].shape[0] < n_atoms or b["shift"].shape[0] < nm:
+            cap = max(n_atoms, 1024 if b is None else b["xyz"].shape[0])
+            capm = max(nm, 16 if b is None else b["shift"].shape[0])
+            b = {"xyz": torch.empty((cap, 3), dtype=torch.float32, device=dev),
+                 "z": torch.empty(cap, dtype=torch.int32, device=dev),
+                 "off": torch.empty(capm + 1, dtype=torch.int32, device=dev),
+                 "shift": torch.empty((capm, 3), dtype=torch.float32, device=dev),
+                 "space": torch.empty((capm, 3), dtype=torch.float32, device=dev),
+                 "present": torch.empty((capm, 4), dtype=torch.int32, device=dev),
+                 "busy": None}
+            bufs[buf_key] = b
+            self._graphs.drop(buf_key)
+        return b
+
+    def _group_work(self, key, idx, ss, uz, dfs, xyz, zz, off, shift, nm):
+        """The device work of one group (slices and images) as prepared launches, and
+        whether it can be captured (the atoms path; the host-side slice build is not)."""
+        m = self.microscope
+        n1, n2 = key[-2:]
+        b = backend.MultiSlicesBuilder(uz, ss[0], n1, n2, self.slice_thickness, self._pixel_size, self._pixel_size)
+        wp = self._propagator((n1, n2))
+        ragged = ss[0] != ss[-1]
+        if not b.atoms_path:
+            def host_work():
+                stack = torch.stack([self.build_slices(self._mols_now[i]) for i in idx])
+                return wp.image(stack, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture,
+                                n_batch=len(idx))
+            return [host_work], False
+        # too large a stack to hold: slices built a few pairs at a time
+        if not ragged and 4 * len(idx) * ss[0] * n1 * n2 > _STACK_LIMIT_BYTES:
+            return [backend.prepare_image_from_device_atoms(
+                b, wp, xyz, zz, off, shift, idx, nm, m.electron_dose, m.cs_mm, dfs, m.aperture,
+                slice_chunk_pairs(len(idx), n1, n2))], True
+        build = backend.prepare_build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, nm,
+                                                               slot_slices=ss if ragged else None)
+        if ragged:
+            image = backend.prepare_image_ragged(wp, build.result, ss, self.slice_thickness, m.electron_dose, m.cs_mm,
+                                                 dfs, m.aperture)
+        else:
+            image = wp.prepare_image(build.result, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture,
+                                     n_batch=len(idx))
+        return [build, image], True
+
+    def _launch_chunk(self, mols, defocus, rois, buf_key=None):
         """Queue the device work of one chunk on the current stream (groups of other
         lateral sizes on side streams joined back into it); returns [(indices, images)]."""
         m = self.microscope
@@ -298,12 +402,26 @@ class Pipe:
         n_atoms = int(offsets[-1])
         hx, hz = self._stage(n_atoms)
         self._fill_stage(mols, offsets, hx.numpy(), hz.numpy())
-        xyz = hx.to(dev, non_blocking=True)
-        zz = hz.to(dev, non_blocking=True)
-        off = torch.from_numpy(offsets.astype(np.uint32).view(np.int32)).to(dev)
-        shift = torch.empty((nm, 3), dtype=torch.float32, device=dev)
-        space = torch.empty((nm, 3), dtype=torch.float32, device=dev)
-        present = torch.empty((nm, 4), dtype=torch.int32, device=dev)
+        graphs = self.cuda_graphs and buf_key is not None
+        main = torch.cuda.current_stream()
+        off_h = torch.from_numpy(offsets.astype(np.uint32).view(np.int32))
+        if graphs:
+            bufs = self._inputs(buf_key, n_atoms, nm)
+            if bufs["busy"] is not None:
+                main.wait_event(bufs["busy"])  # the last batch on these buffers is done with them
+            xyz, zz = bufs["xyz"][:n_atoms], bufs["z"][:n_atoms]
+            off, shift = bufs["off"][:nm + 1], bufs["shift"][:nm]
+            space, present = bufs["space"][:nm], bufs["present"][:nm]
+            xyz.copy_(hx, non_blocking=True)
+            zz.copy_(hz, non_blocking=True)
+            off.copy_(off_h)
+        else:
+            xyz = hx.to(dev, non_blocking=True)
+            zz = hz.to(dev, non_blocking=True)
+            off = off_h.to(dev)
+            shift = torch.empty((nm, 3), dtype=torch.float32, device=dev)
+            space = torch.empty((nm, 3), dtype=torch.float32, device=dev)
+            present = torch.empty((nm, 4), dtype=torch.int32, device=dev)
         P = backend._ptr
         backend._native.call("emsim_gb300_centralize", P(xyz), P(zz), P(off), nm, P(shift), P(space), P(present),
                              backend._stream())
@@ -321,53 +439,80 @@ class Pipe:
             n_sl[i] = ns
             fast = _fast_len(n1) and _fast_len(n2)
             groups[(n1, n2) if fast else (ns, n1, n2)].append(i)
-        main = torch.cuda.current_stream()
-        ready = torch.cuda.Event()
-        ready.record(main)
-        side, done = [], []
+        plan = []
         for key, idx in groups.items():
-            n1, n2 = key[-2:]
             idx = sorted(idx, key=lambda i: -n_sl[i])  # longest stack first
             ss = [n_sl[i] for i in idx]
             union = np.bitwise_or.reduce(mask_h[idx], axis=0)
             uz = [32 * w + b for w in range(4) for b in range(32) if (int(union[w]) >> b) & 1]
-            dfs = [m.defocus if defocus is None else defocus[i] for i in idx]
-            # lateral sizes overlap on the GPU: each group runs on its own stream
-            st = torch.cuda.Stream() if len(groups) > 1 else main
-            st.wait_event(ready)
-            with torch.cuda.stream(st):
-                b = backend.MultiSlicesBuilder(uz, ss[0], n1, n2, self.slice_thickness, self._pixel_size,
-                                               self._pixel_size)
-                wp = self._propagator((n1, n2))
-                ragged = ss[0] != ss[-1]
-                # too large a stack to hold: slices built a few pairs at a time
-                chunked = b.atoms_path and not ragged and 4 * len(idx) * ss[0] * n1 * n2 > _STACK_LIMIT_BYTES
-                if chunked:
-                    imgs = backend.image_from_device_atoms(b, wp, xyz, zz, off, shift, idx, nm, m.electron_dose,
-                                                           m.cs_mm, dfs, m.aperture,
-                                                           slice_chunk_pairs(len(idx), n1, n2))
-                elif b.atoms_path:
-                    stack = backend.build_slices_from_device_atoms(b, xyz, zz, off, shift, idx, nm,
-                                                                   slot_slices=ss if ragged else None)
-                else:
-                    stack = torch.stack([self.build_slices(mols[i]) for i in idx])
-                if chunked:
-                    pass
-                elif ragged:
-                    imgs = backend.image_ragged(wp, stack, ss, self.slice_thickness, m.electron_dose, m.cs_mm, dfs,
-                                                m.aperture)
-                else:
-                    imgs = wp.image(stack, self.slice_thickness, m.electron_dose, m.cs_mm, dfs, m.aperture,
-                                    n_batch=len(idx))
-                imgs = imgs.reshape(len(idx), n1, n2)
+            dfs = [float(m.defocus if defocus is None else defocus[i]) for i in idx]
+            plan.append((key, idx, ss, uz, dfs))
+        self._mols_now = mols  # read by the host-side slice build of groups off the atoms path
+        try:
+            if graphs:
+                done = self._graph_chunk(buf_key, plan, n_atoms, nm, xyz, zz, off, shift, main)
+                if done is not None:
+                    ev = torch.cuda.Event()
+                    ev.record(main)
+                    bufs["busy"] = ev
+                    return done
+            ready = torch.cuda.Event()
+            ready.record(main)
+            side, done = [], []
+            for key, idx, ss, uz, dfs in plan:
+                # lateral sizes overlap on the GPU: each group runs on its own stream
+                st = torch.cuda.Stream() if len(plan) > 1 else main
+                st.wait_event(ready)
+                with torch.cuda.stream(st):
+                    work, _ = self._group_work(key, idx, ss, uz, dfs, xyz, zz, off, shift, nm)
+                    for w in work:
+                        imgs = w()
+                    imgs = backend._wrap(imgs.reshape(len(idx), *key[-2:]))
+                    if st is not main:
+                        imgs.record_stream(main)
                 if st is not main:
-                    imgs.record_stream(main)
-            if st is not main:
-                side.append(st)
-            done.append((idx, imgs))
-        for st in side:
-            main.wait_stream(st)
-        return done
+                    side.append(st)
+                done.append((idx, imgs))
+            for st in side:
+                main.wait_stream(st)
+            if graphs:
+                ev = torch.cuda.Event()
+                ev.record(main)
+                bufs["busy"] = ev
+            return done
+        finally:
+            self._mols_now = None
+
+    def _graph_chunk(self, buf_key, plan, n_atoms, nm, xyz, zz, off, shift, main):
+        """The chunk's groups through a CUDA graph: replayed if this structure was
+        captured, captured on its second sighting, else None (run it eagerly).  Images
+        come back as copies, so that the next replay does not overwrite them."""
+        m = self.microscope
+        key = (n_atoms, nm, tuple((k, tuple(idx), tuple(ss), tuple(uz), tuple(dfs)) for k, idx, ss, uz, dfs in plan),
+               (float(m.electron_dose), float(m.cs_mm), float(m.aperture), float(m.wave_length)),
+               float(self.slice_thickness), float(self._pixel_size), backend.get_precision())
+        ent = self._graphs.get(buf_key, key)
+        if ent is None:
+            if self._graphs.sighting(buf_key, key) < 2:
+                return None
+            work = []
+            for k, idx, ss, uz, dfs in plan:
+                w, ok = self._group_work(k, idx, ss, uz, dfs, xyz, zz, off, shift, nm)
+                if not ok:
+                    return None
+                work.append((k, idx, w))
+            cap = self._chunk_stream((buf_key, "capture"))
+            cap.wait_stream(main)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=cap):
+                for _, _, w in work:
+                    for step in w:
+                        step()
+            main.wait_stream(cap)
+            ent = {"graph": g, "work": work}
+            self._graphs.put(buf_key, key, ent)
+        ent["graph"].replay()
+        return [(idx, backend._wrap(w[-1].result.reshape(len(idx), *k[-2:]).clone())) for k, idx, w in ent["work"]]
 
     def _run_batch_host(self, mols, defocus=None) -> List:
         """run_batch with the front-end on the host (voxel water needs the histograms) or

@@ -396,3 +396,17 @@ def test_register_with_the_reference_emsim_config():
     finally:
         em.config.set_backend("numpy")
     assert em.config.get_current_backend().wave_propagator.__module__.endswith("wave_propagator_numpy")
+
+
+def test_pipe_graph_cache_sightings_lru_and_drop():
+    from emsim_gb300.pipe import _GraphCache
+    c = _GraphCache(max_entries=2)
+    assert c.sighting("a", 1) == 1 and c.sighting("a", 1) == 2 and c.sighting("b", 1) == 1
+    c.put("a", 1, "g1")
+    c.put("a", 2, "g2")
+    assert c.get("a", 1) == "g1"  # now the most recently used
+    c.put("a", 3, "g3")           # drops key 2, the least recently used
+    assert c.get("a", 2) is None and c.get("a", 1) == "g1" and c.get("a", 3) == "g3"
+    assert c.get("b", 1) is None and len(c) == 2
+    c.drop("a")                   # the buffer set grew: its graphs and sightings go
+    assert len(c) == 0 and c.sighting("a", 1) == 1 and c.sighting("b", 1) == 2
