@@ -21,13 +21,21 @@ Contents
       ``slice_builder_base.py``): ``linspace`` q-grid, numpy histogram binning rule,
       strict aperture, complex128 arithmetic.
 
-``oracle.ref_numpy``  imports the reference's own numpy path (only where the reference
-    tree exists, i.e. never on a GPU host) to generate golden vectors.
+``oracle.ref_numpy``  imports the reference's own numpy path, or its FFTW backend with
+    the extension that ``oracle.ref_fftw`` builds (only where the reference tree exists,
+    i.e. never on a GPU host) to generate golden vectors.
+
+``oracle.ref_fftw``  builds emsim's FFTW extension from the reference C++ sources into
+    ``oracle/_ref``, against the oracle's own FFTW-interface transforms (``fftw3.h``,
+    ``fftw_stub.cpp``) in place of the absent libfftw3f.
 
 Parity status: PINNED.  ``tests/golden/make_golden.py`` ran the reference's own numpy
 path on seeded small inputs; ``tests/test_oracle_golden.py`` checks the ``"numpy"``
 semantics against those vectors (bit-exact for binning, ~1e-12 for floating point).
 The ``"fftw"`` semantics shares every helper with the pinned path and differs only by
 the documented reference deltas (frequency grid, filter placement, aperture test,
-binning start edge), each tested separately.
+binning start edge), each tested separately, and is PINNED too:
+``tests/golden/make_golden_fftw.py`` ran the reference's FFTW extension (compiled from
+its C++) through its FFTW backend, and ``tests/test_oracle_ref_fftw.py`` checks the FP32
+restatement against those vectors to float rounding.
 """

@@ -1,4 +1,5 @@
-"""Import the reference emsim package (numpy backend) from its source tree.
+"""Import the reference emsim package (numpy backend, or its FFTW backend with the
+extension built by ``oracle/ref_fftw/build.py``) from its source tree.
 
 Test infrastructure only, and usable only where the reference tree exists (the
 development container; never a GPU host).  Its location comes from the environment
@@ -56,3 +57,30 @@ def load():
     logging.getLogger("emsim").setLevel(logging.WARNING)
     emsim.config.set_backend("numpy")
     return emsim
+
+
+def load_fftw():
+    """Return the reference ``emsim`` package with its FFTW backend selected: the
+    extension modules ``wave_kernel`` / ``slice_kernel``, compiled from the reference's
+    C++ by ``oracle.ref_fftw.build`` (built on first use), take the place of the
+    package files ``emsim.backend.fftw_ext`` would hold."""
+    import importlib.machinery
+    import importlib.util
+
+    em = load()
+    from oracle.ref_fftw import build as rb
+    mods = rb.built()
+    if len(mods) < 2:
+        mods = rb.build(reference_root())
+    import emsim.backend.fftw_ext as ext
+    for name, path in mods.items():
+        full = f"emsim.backend.fftw_ext.{name}"
+        if full not in sys.modules:
+            loader = importlib.machinery.ExtensionFileLoader(full, str(path))
+            spec = importlib.util.spec_from_file_location(full, str(path), loader=loader)
+            mod = importlib.util.module_from_spec(spec)
+            loader.exec_module(mod)
+            sys.modules[full] = mod
+        setattr(ext, name, sys.modules[full])
+    em.config.set_backend("fftw")
+    return em
