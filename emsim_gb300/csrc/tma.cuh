@@ -138,5 +138,26 @@ __device__ __forceinline__ void tensor_g2s_2d(void* dst, const CUtensorMap* map,
         : "memory");
 }
 
+// 2-D tiled tensor copy of one box from shared memory to global element coordinates
+// (x, y) (both >= 0, x * element size a multiple of 16 bytes), in the issuing thread's
+// bulk async-group
+__device__ __forceinline__ void tensor_s2g_2d(const CUtensorMap* map, int x, int y, const void* src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the issuing thread's bulk groups: wait until at most N of them still read shared memory
+// (READ) or are incomplete; they are the thread's own copies, which always finish
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+template <int N>
+__device__ __forceinline__ void bulk_wait() {
+    asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
+}
+
 }  // namespace tma
 }  // namespace emsim_gb300
