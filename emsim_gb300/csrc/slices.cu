@@ -219,7 +219,7 @@ int generic_build(emsim_gb300_slice_plan* p, const SliceArgs& a, cudaStream_t st
 // Workspace of build_slices for n_atoms atoms of n_img images, carved in this order
 // (each piece 256-byte aligned).
 struct AtomsWorkspace {
-    size_t group_start, group_tmp, bucket, item, count, off, cursor, bucket_tmp, items, work, total;
+    size_t group_start, group_tmp, bucket, item, count, off, cursor, bucket_tmp, items, tile_counter, work, total;
     long long n_buckets;
 };
 
@@ -247,6 +247,7 @@ AtomsWorkspace atoms_workspace(const emsim_gb300_slice_plan* p, unsigned n_atoms
     w.cursor = take(sizeof(unsigned) * (size_t)w.n_buckets);
     w.bucket_tmp = take(sizeof(unsigned) * scan_tmp_words(w.n_buckets));
     w.items = take(sizeof(unsigned) * (size_t)n_atoms);
+    w.tile_counter = take(sizeof(unsigned));
     w.work = take(sizeof(float2) * (size_t)n_img * work_pairs * p->n1 * p->n2);
     w.total = o;
     return w;
@@ -295,6 +296,7 @@ int bucket_atoms_z(emsim_gb300_slice_plan* p, const float* coords, const int32_t
     a.n2 = p->n2;
     a.bucket_off = U(w.off);
     a.items = U(w.items);
+    a.tile_counter = U(w.tile_counter);
     a.wq = p->wq;
     a.live_lo = p->col_cut + 1;
     a.live_hi = p->col_cut > 0 ? p->col_cut : 0;
@@ -478,6 +480,7 @@ int emsim_gb300_build_slices(emsim_gb300_slice_plan* p, const float* coords, uns
     a.n_img = n_batch;
     a.bucket_off = U(w.off);
     a.items = U(w.items);
+    a.tile_counter = U(w.tile_counter);
     a.wq = p->wq;
     a.live_lo = p->col_cut + 1;
     a.live_hi = p->col_cut > 0 ? p->col_cut : 0;
