@@ -3,7 +3,7 @@
 //
 // Every atom is binned with the reference's CUDA rule (binning.cuh) - the same integer
 // (slice, row, column) the dense histogram uses - and becomes one 32-bit item
-// (slice parity << 31 | column) in its bucket.  Bucket sizes come from integer atomics;
+// (slice parity << 31 | row << 12 | column) in its bucket.  Bucket sizes come from integer atomics;
 // the scatter places items with an atomic cursor, so the order inside a bucket is not
 // fixed, but everything downstream only forms order-independent exact sums over a
 // bucket (see slice_cols_atoms_kernel), which keeps the slices bit-deterministic.
@@ -125,7 +125,7 @@ __global__ void atoms_bucket_kernel(AtomBucketArgs a) {
             int s, i, j;
             if (bin_axis(z, a.ax0, s) && bin_axis(x, a.ax1, i) && bin_axis(y, a.ax2, j)) {
                 bk = (unsigned)(((long long)lo * a.n_pairs + (s >> 1)) * plane + i);
-                item = ((unsigned)(s & 1) << 31) | (unsigned)j;
+                item = ((unsigned)(s & 1) << 31) | ((unsigned)i << 12) | (unsigned)j;
                 atomicAdd(a.bucket_count + bk, 1u);
             }
         }
@@ -175,7 +175,7 @@ __global__ void atoms_bucket_z_kernel(AtomBucketZArgs a) {
             int s, i, j;
             if (bin_axis(z, az, s) && bin_axis(x, a.ax1, i) && bin_axis(y, a.ax2, j)) {
                 bk = (unsigned)((((long long)slot * a.n_elems + e) * a.n_pairs + (s >> 1)) * plane + i);
-                item = ((unsigned)(s & 1) << 31) | (unsigned)j;
+                item = ((unsigned)(s & 1) << 31) | ((unsigned)i << 12) | (unsigned)j;
                 atomicAdd(a.bucket_count + bk, 1u);
             }
         }

@@ -18,6 +18,7 @@
 #include "fft16.cuh"
 #include "slices.h"
 #include "wave_passes.cuh"
+#include "wave_r16.cuh"
 
 namespace emsim_gb300 {
 
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
                 int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
                 for (unsigned k = lo; k < hi; ++k) {
                     const unsigned u = items[k];
-                    const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
+                    const int idx = ((int)(u & 0xfffu) * col) & kmask;
                     const int2 w = wq[idx + (idx >> 4)];
                     const bool odd = (u >> 31) != 0;  // the odd slice of the pair: i W^m
                     re += odd ? -w.y : w.x;
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
                 long long re = 0, im = 0;
                 for (unsigned k = lo; k < hi; ++k) {
                     const unsigned u = items[k];
-                    const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
+                    const int idx = ((int)(u & 0xfffu) * col) & kmask;
                     const int2 w = wq[idx + (idx >> 4)];
                     const bool odd = (u >> 31) != 0;
                     re += odd ? -w.y : w.x;
@@ -184,26 +185,39 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     for (int m = 0; m < 8; ++m) dst[(long long)(t + m * T) * ld] = acc[m];
 }
 
-// The same pass as persistent CTAs that take runs of `run` consecutive live column tiles,
-// in (image, slice pair, tile) order, from a work queue (an atomic counter), so that
-// planes of uneven atom counts and stacks of uneven slice counts balance over the SMs.
-// The W_n2 table is staged once per CTA, and a slice pair's bucket offsets (every
-// element) and items once per run instead of once per tile: the tiles of a pair read the
-// same atoms, so a 4-column tile no longer starts with a round trip to L2 for them; each
-// element's filter column is loaded before its sums and transform, which hide the load.
-// Dead tiles (outside the filters' support) are written as zeros after the live ones.
-// Results are bitwise those of the per-tile form.
 constexpr int OFF_CACHE_BYTES = 40 * 1024;  // bucket offsets of every element of one pair
 
 int persistent_grid(const void* func, int threads, size_t smem, int n_tiles);
 
+// From length 512 the same pass runs as persistent CTAs of 512 threads with 16 values per
+// thread (the radix-16 column transforms of the wave passes, twiddles staged in shared
+// memory up to 2048).  They take runs of `run` consecutive live column tiles, in (image,
+// slice pair, tile) order, from a work queue (an atomic counter), so that planes of
+// uneven atom counts and stacks of uneven slice counts balance over the SMs.  The W_n2
+// table is staged once per CTA, and a pair's bucket offsets (every element) and items
+// once per pair and CTA instead of once per tile.  The row transforms of the atoms are
+// summed per atom: each thread takes atoms of the plane, looks up W^(j k2) for the tile's
+// B columns and adds the fixed-point entries into (column, row) slots with integer
+// shared-memory atomics, so the work is uniform over the atoms and no warp waits for the
+// longest of its rows' buckets; the sums are the same integers as the per-row ones.  A
+// plane with a row bucket above WQ_SMALL atoms takes 64-bit per-row sums instead.  Dead
+// tiles (outside the filters' support) are written as zeros after the live ones.
 template <int N>
-__global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
-    slice_cols_atoms_persist_kernel(SliceArgs a, int lt_lo, int lt_hi, int run) {
-    constexpr int T = N / 8;
+struct ColAtoms16 {
+    static constexpr int T = N / 16;
+    static constexpr int B = 512 / T;        // columns per tile
+    static constexpr int PAD = 32 / B;       // sum slots: column b at b (N + PAD), conflict-free reads
+    static constexpr int STRIDE = N + PAD;
+    static constexpr int TW = r16::col_tw_entries<N>();
+};
+
+template <int N>
+__global__ void __launch_bounds__(512, 1) slice_cols_atoms16_kernel(SliceArgs a, int lt_lo, int lt_hi, int run) {
+    using C = ColAtoms16<N>;
+    constexpr int T = C::T;
+    constexpr int B = C::B;
     constexpr float INV_SCALE = (float)(1.0 / WQ_SCALE);
-    extern __shared__ float2 sm[];
-    const int B = blockDim.x / T;
+    extern __shared__ __align__(16) float2 sm[];
     const int b = threadIdx.x & (B - 1);
     const int t = threadIdx.x / B;
     const int E = a.n_elems;
@@ -212,11 +226,20 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
     const int live = lt_lo + lt_hi;
     const long long npix = (long long)N * a.n2;
     const long long ld = a.n2;
-    ColAddrRt addr{B};
-    int2* wq = reinterpret_cast<int2*>(sm + (N + N / 8) * B);
+    // shared memory: exchange slots / integer sums, twiddles, the padded W_n2 table, the
+    // pair's bucket offsets for every element, one flag per element (a row bucket above
+    // WQ_SMALL), the staged items
+    float2* xbuf = sm;
+    float2* s_tw = xbuf + B * C::STRIDE;
+    int2* wq = reinterpret_cast<int2*>(s_tw + C::TW);
     unsigned* s_off = reinterpret_cast<unsigned*>(wq + a.n2 + a.n2 / 16 + 1);  // E x (N + 1)
-    unsigned* s_items = s_off + E * (N + 1);
+    int* s_big = reinterpret_cast<int*>(s_off + E * (N + 1));
+    unsigned* s_items = reinterpret_cast<unsigned*>(s_big + E);
+    int* acc_re = reinterpret_cast<int*>(xbuf);
+    int* acc_im = acc_re + B * C::STRIDE;
+    for (int i = threadIdx.x; i < C::TW; i += blockDim.x) s_tw[i] = __ldg(a.tw + i * (fft::TW_SIZE / N));
     for (int i = threadIdx.x; i < a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
+    const fft16::ColSlot addr{B, B >= 16 ? 0 : (16 / B) - 1};
     const int kmask = a.n2 - 1;
     __shared__ unsigned s_run;
     const long long n_live = (long long)a.n_img * P * live;
@@ -238,8 +261,6 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
             const int pair = a.pair0 + (int)(y - (long long)img * P);
             if (a.img_slices && 2 * pair >= a.img_slices[img]) continue;  // past this image's stack
             if (y != cur_y) {
-                // stage the pair's offsets for every element, then (if they fit) its items,
-                // element after element
                 __syncthreads();  // every thread is done with the previous pair's offsets and items
                 for (int e = 0; e < E; ++e) {
                     const unsigned* off_g = a.bucket_off + ((long long)(img * E + e) * a.n_pairs + pair) * N;
@@ -253,50 +274,67 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
                     unsigned at = 0;
                     for (int e = 0; e < E; ++e) {
                         const unsigned base = s_off[e * (N + 1)], count = s_off[e * (N + 1) + N] - base;
-                        for (unsigned i = threadIdx.x; i < count; i += blockDim.x) s_items[at + i] = __ldg(a.items + base + i);
+                        for (unsigned i = threadIdx.x; i < count; i += blockDim.x)
+                            s_items[at + i] = __ldg(a.items + base + i);
                         at += count;
                     }
+                }
+                for (int e = 0; e < E; ++e) {
+                    bool big = false;
+                    const unsigned* off = s_off + e * (N + 1);
+                    for (int r = threadIdx.x; r < N; r += blockDim.x) big |= (off[r + 1] - off[r]) > (unsigned)WQ_SMALL;
+                    const int any = __syncthreads_or(big);
+                    if (threadIdx.x == 0) s_big[e] = any;
                 }
                 __syncthreads();
                 cur_y = y;
             }
             const int col = ct * B + b;
-            float2 acc[8];
-    #pragma unroll
-            for (int m = 0; m < 8; ++m) acc[m] = make_float2(0.f, 0.f);
+            const int c0 = ct * B;
+            float2 acc[16];
+#pragma unroll
+            for (int m = 0; m < 16; ++m) acc[m] = make_float2(0.f, 0.f);
             unsigned at = 0;  // this element's first item in the staged items
             for (int e = 0; e < E; ++e) {
                 const unsigned* off = s_off + e * (N + 1);
                 const unsigned base = off[0], count = off[N] - base;
-                const unsigned* items = cached ? s_items + at : a.items + base;  // indexed from the plane's first item
+                const unsigned* items = cached ? s_items + at : a.items + base;  // from the plane's first item
                 at += count;
                 if (count == 0) continue;  // an element without atoms in this slice pair adds exactly zero
-                // the filter column, loaded before the sums and the transform hide its latency
-                const float* te = a.filt + (long long)e * npix + col;
-                float f[8];
-    #pragma unroll
-                for (int m = 0; m < 8; ++m) f[m] = __ldg(te + (long long)(t + m * T) * ld);
-                float2 v[8];
-    #pragma unroll
-                for (int m = 0; m < 8; ++m) {
-                    const int r = t + m * T;
-                    const unsigned lo = off[r] - base, hi = off[r + 1] - base;
-                    if (hi - lo <= (unsigned)WQ_SMALL) {
-                        int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
-                        for (unsigned k = lo; k < hi; ++k) {
-                            const unsigned u = items[k];
-                            const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
+                float2 v[16];
+                if (!s_big[e]) {
+                    int4* z4 = reinterpret_cast<int4*>(acc_re);
+                    for (int i = threadIdx.x; i < B * C::STRIDE / 2; i += blockDim.x) z4[i] = make_int4(0, 0, 0, 0);
+                    __syncthreads();
+                    // exact: every (column, row) slot sums at most WQ_SMALL entries below 2^22
+                    for (unsigned k = threadIdx.x; k < count; k += blockDim.x) {
+                        const unsigned u = items[k];
+                        const int r = (int)((u >> 12) & 0xfffu), jj = (int)(u & 0xfffu);
+                        const bool odd = (u >> 31) != 0;  // the odd slice of the pair: i W^m
+                        int idx = (jj * c0) & kmask;
+#pragma unroll 4
+                        for (int bb = 0; bb < B; ++bb) {
                             const int2 w = wq[idx + (idx >> 4)];
-                            const bool odd = (u >> 31) != 0;  // the odd slice of the pair: i W^m
-                            re += odd ? -w.y : w.x;
-                            im += odd ? w.x : w.y;
+                            atomicAdd(acc_re + bb * C::STRIDE + r, odd ? -w.y : w.x);
+                            atomicAdd(acc_im + bb * C::STRIDE + r, odd ? w.x : w.y);
+                            idx = (idx + jj) & kmask;
                         }
-                        v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
-                    } else {
+                    }
+                    __syncthreads();
+#pragma unroll
+                    for (int m = 0; m < 16; ++m) {
+                        const int o = b * C::STRIDE + t + m * T;
+                        v[m] = make_float2((float)acc_re[o] * INV_SCALE, (float)acc_im[o] * INV_SCALE);
+                    }
+                    __syncthreads();  // the sums are read: the slots become the exchange buffer
+                } else {
+#pragma unroll
+                    for (int m = 0; m < 16; ++m) {
+                        const int r = t + m * T;
                         long long re = 0, im = 0;
-                        for (unsigned k = lo; k < hi; ++k) {
+                        for (unsigned k = off[r] - base; k < off[r + 1] - base; ++k) {
                             const unsigned u = items[k];
-                            const int idx = ((int)(u & 0x7fffffffu) * col) & kmask;
+                            const int idx = ((int)(u & 0xfffu) * col) & kmask;
                             const int2 w = wq[idx + (idx >> 4)];
                             const bool odd = (u >> 31) != 0;
                             re += odd ? -w.y : w.x;
@@ -305,17 +343,19 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
                         v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
                     }
                 }
-                fft::fft_regs<N, false, false>(v, sm, b, t, addr, a.tw);
-    #pragma unroll
-                for (int m = 0; m < 8; ++m) {
-                    acc[m].x = fmaf(f[m], v[m].x, acc[m].x);
-                    acc[m].y = fmaf(f[m], v[m].y, acc[m].y);
+                r16::fft_col<N, false>(v, xbuf, b, t, addr, a.tw, s_tw);
+                const float* te = a.filt + (long long)e * npix + col;
+#pragma unroll
+                for (int m = 0; m < 16; ++m) {
+                    const float f = __ldg(te + (long long)(t + m * T) * ld);
+                    acc[m].x = fmaf(f, v[m].x, acc[m].x);
+                    acc[m].y = fmaf(f, v[m].y, acc[m].y);
                 }
             }
-            fft::fft_regs<N, true, false>(acc, sm, b, t, addr, a.tw);
+            r16::fft_col<N, true>(acc, xbuf, b, t, addr, a.tw, s_tw);
             float2* dst = a.work + y * npix + col;
-    #pragma unroll
-            for (int m = 0; m < 8; ++m) dst[(long long)(t + m * T) * ld] = acc[m];
+#pragma unroll
+            for (int m = 0; m < 16; ++m) dst[(long long)(t + m * T) * ld] = acc[m];
         }
     }
     // the tiles outside the filters' support: zero spectra
@@ -329,7 +369,7 @@ __global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
         const int col = (lt_lo + (int)(d - y * dead)) * B + b;
         float2* dst = a.work + y * npix + col;
 #pragma unroll
-        for (int m = 0; m < 8; ++m) dst[(long long)(t + m * T) * ld] = make_float2(0.f, 0.f);
+        for (int m = 0; m < 16; ++m) dst[(long long)(t + m * T) * ld] = make_float2(0.f, 0.f);
     }
 }
 
@@ -338,29 +378,34 @@ int slice_cols_atoms_n(const SliceArgs& a, cudaStream_t st) {
     constexpr int T = N / 8;
     const int B = col_B_for(N, a.n2);
     const size_t off_bytes = (size_t)a.n_elems * (N + 1) * sizeof(unsigned);
-    // persistent from length 512 (1.07x the per-tile form at 2048^2, 1.04x on 512^2 blobs;
-    // 0.96x on 256^2 blobs, whose many small CTAs already overlap their staging)
-    if (N >= 512 && off_bytes <= (size_t)OFF_CACHE_BYTES && a.tile_counter != nullptr) {
-        const int tiles = a.n2 / B;
-        int lt_lo = (a.live_lo + B - 1) / B, lt_hi = (a.live_hi + B - 1) / B;
-        if (a.live_lo < 0 || a.live_hi < 0) lt_lo = lt_hi = 0;
-        if (lt_lo + lt_hi >= tiles) {
-            lt_lo = tiles;
-            lt_hi = 0;
+    // persistent with 16 values per thread from length 512 (1.15x the per-tile form at
+    // 2048^2 and on 512^2 blobs); the per-tile form below 512, where its many small CTAs
+    // already overlap their staging
+    if constexpr (N >= 512) {
+        using C = ColAtoms16<N>;
+        if (off_bytes <= (size_t)OFF_CACHE_BYTES && a.tile_counter != nullptr && a.n2 >= C::B) {
+            const int tiles = a.n2 / C::B;
+            int lt_lo = (a.live_lo + C::B - 1) / C::B, lt_hi = (a.live_hi + C::B - 1) / C::B;
+            if (a.live_lo < 0 || a.live_hi < 0) lt_lo = lt_hi = 0;
+            if (lt_lo + lt_hi >= tiles) {
+                lt_lo = tiles;
+                lt_hi = 0;
+            }
+            const size_t smem = ((size_t)C::B * C::STRIDE + C::TW) * sizeof(float2) +
+                                (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) + off_bytes + a.n_elems * sizeof(int) +
+                                (size_t)ITEM_CACHE * sizeof(unsigned);
+            const void* k = (const void*)slice_cols_atoms16_kernel<N>;
+            EMSIM_TRY(ensure_smem_attr(k, smem));
+            const long long n_tiles = (long long)a.n_img * a.pairs_here() * tiles;
+            const int grid = persistent_grid(k, 512, smem, (int)(n_tiles < (1 << 30) ? n_tiles : (1 << 30)));
+            // runs of up to 16 tiles of one pair: a handful of queue operations per pair
+            const int live = lt_lo + lt_hi;
+            const int run = live < 16 ? (live > 0 ? live : 1) : 16;
+            EMSIM_CHECK_CUDA(cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned), st));
+            slice_cols_atoms16_kernel<N><<<grid, 512, smem, st>>>(a, lt_lo, lt_hi, run);
+            EMSIM_CHECK_LAUNCH();
+            return EMSIM_GB300_OK;
         }
-        const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) +
-                            off_bytes + (size_t)ITEM_CACHE * sizeof(unsigned);
-        const void* k = (const void*)slice_cols_atoms_persist_kernel<N>;
-        EMSIM_TRY(ensure_smem_attr(k, smem));
-        const long long n_tiles = (long long)a.n_img * a.pairs_here() * tiles;
-        const int grid = persistent_grid(k, B * T, smem, (int)(n_tiles < (1 << 30) ? n_tiles : (1 << 30)));
-        // runs of up to 16 tiles of one pair: a handful of queue operations per pair
-        const int live = lt_lo + lt_hi;
-        const int run = live < 16 ? (live > 0 ? live : 1) : 16;
-        EMSIM_CHECK_CUDA(cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned), st));
-        slice_cols_atoms_persist_kernel<N><<<grid, B * T, smem, st>>>(a, lt_lo, lt_hi, run);
-        EMSIM_CHECK_LAUNCH();
-        return EMSIM_GB300_OK;
     }
     const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) + (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) +
                         (size_t)(N + 1 + ITEM_CACHE) * sizeof(unsigned);

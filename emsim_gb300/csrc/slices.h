@@ -15,7 +15,7 @@ struct SliceArgs {
     int n_img = 1;  // slice stacks in the call (work / out hold n_img stacks back to back)
     // bucketed atoms (build from atoms)
     const unsigned* bucket_off = nullptr;  // (n_img * n_elems * n_pairs * n1 + 1) start offsets into items
-    const unsigned* items = nullptr;       // (slice parity << 31) | column, grouped by bucket
+    const unsigned* items = nullptr;       // (slice parity << 31) | (row << 12) | column, grouped by bucket
     const int2* wq = nullptr;              // W_n2^m then i W_n2^m, m < n2, WQ_SCALE fixed point
     const int* img_slices = nullptr;       // per image slice count (<= n_slices); pairs beyond are skipped
     unsigned* tile_counter = nullptr;      // one word of device scratch: the column pass's work queue
