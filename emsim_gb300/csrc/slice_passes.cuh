@@ -189,6 +189,151 @@ constexpr int OFF_CACHE_BYTES = 40 * 1024;  // bucket offsets of every element o
 
 int persistent_grid(const void* func, int threads, size_t smem, int n_tiles);
 
+// The same pass as persistent CTAs that take runs of `run` consecutive live column tiles,
+// in (image, slice pair, tile) order, from a work queue (an atomic counter), so that
+// planes of uneven atom counts and stacks of uneven slice counts balance over the SMs.
+// The W_n2 table is staged once per CTA, and a slice pair's bucket offsets (every
+// element) and items once per run instead of once per tile: the tiles of a pair read the
+// same atoms, so a 4-column tile no longer starts with a round trip to L2 for them; each
+// element's filter column is loaded before its sums and transform, which hide the load.
+// Dead tiles (outside the filters' support) are written as zeros after the live ones.
+// Results are bitwise those of the per-tile form.
+template <int N>
+__global__ void __launch_bounds__(ColThreads<N>::MAX, ColThreads<N>::MIN_BLOCKS)
+    slice_cols_atoms_persist_kernel(SliceArgs a, int lt_lo, int lt_hi, int run) {
+    constexpr int T = N / 8;
+    constexpr float INV_SCALE = (float)(1.0 / WQ_SCALE);
+    extern __shared__ float2 sm[];
+    const int B = blockDim.x / T;
+    const int b = threadIdx.x & (B - 1);
+    const int t = threadIdx.x / B;
+    const int E = a.n_elems;
+    const int P = a.pairs_here();
+    const int tiles = a.n2 / B;
+    const int live = lt_lo + lt_hi;
+    const long long npix = (long long)N * a.n2;
+    const long long ld = a.n2;
+    ColAddrRt addr{B};
+    int2* wq = reinterpret_cast<int2*>(sm + (N + N / 8) * B);
+    unsigned* s_off = reinterpret_cast<unsigned*>(wq + a.n2 + a.n2 / 16 + 1);  // E x (N + 1)
+    unsigned* s_items = s_off + E * (N + 1);
+    for (int i = threadIdx.x; i < a.n2; i += blockDim.x) wq[i + (i >> 4)] = a.wq[i];
+    const int kmask = a.n2 - 1;
+    __shared__ unsigned s_run;
+    const long long n_live = (long long)a.n_img * P * live;
+    const long long n_runs = (n_live + run - 1) / run;
+    long long cur_y = -1;
+    bool cached = false;
+    for (;;) {
+        if (threadIdx.x == 0) s_run = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const long long r0 = s_run;
+        __syncthreads();  // every thread has its run before the next one is taken
+        if (r0 >= n_runs) break;
+        const long long g_end = (r0 + 1) * run < n_live ? (r0 + 1) * run : n_live;
+        for (long long g = r0 * run; g < g_end; ++g) {
+            const long long y = g / live;  // img * pairs_here + pair - pair0
+            const int j = (int)(g - y * live);
+            const int ct = j < lt_lo ? j : tiles - lt_hi + (j - lt_lo);
+            const int img = (int)(y / P);
+            const int pair = a.pair0 + (int)(y - (long long)img * P);
+            if (a.img_slices && 2 * pair >= a.img_slices[img]) continue;  // past this image's stack
+            if (y != cur_y) {
+                // stage the pair's offsets for every element, then (if they fit) its items,
+                // element after element
+                __syncthreads();  // every thread is done with the previous pair's offsets and items
+                for (int e = 0; e < E; ++e) {
+                    const unsigned* off_g = a.bucket_off + ((long long)(img * E + e) * a.n_pairs + pair) * N;
+                    for (int i = threadIdx.x; i <= N; i += blockDim.x) s_off[e * (N + 1) + i] = __ldg(off_g + i);
+                }
+                __syncthreads();
+                unsigned total = 0;
+                for (int e = 0; e < E; ++e) total += s_off[e * (N + 1) + N] - s_off[e * (N + 1)];
+                cached = total <= (unsigned)ITEM_CACHE;
+                if (cached) {
+                    unsigned at = 0;
+                    for (int e = 0; e < E; ++e) {
+                        const unsigned base = s_off[e * (N + 1)], count = s_off[e * (N + 1) + N] - base;
+                        for (unsigned i = threadIdx.x; i < count; i += blockDim.x) s_items[at + i] = __ldg(a.items + base + i);
+                        at += count;
+                    }
+                }
+                __syncthreads();
+                cur_y = y;
+            }
+            const int col = ct * B + b;
+            float2 acc[8];
+    #pragma unroll
+            for (int m = 0; m < 8; ++m) acc[m] = make_float2(0.f, 0.f);
+            unsigned at = 0;  // this element's first item in the staged items
+            for (int e = 0; e < E; ++e) {
+                const unsigned* off = s_off + e * (N + 1);
+                const unsigned base = off[0], count = off[N] - base;
+                const unsigned* items = cached ? s_items + at : a.items + base;  // indexed from the plane's first item
+                at += count;
+                if (count == 0) continue;  // an element without atoms in this slice pair adds exactly zero
+                // the filter column, loaded before the sums and the transform hide its latency
+                const float* te = a.filt + (long long)e * npix + col;
+                float f[8];
+    #pragma unroll
+                for (int m = 0; m < 8; ++m) f[m] = __ldg(te + (long long)(t + m * T) * ld);
+                float2 v[8];
+    #pragma unroll
+                for (int m = 0; m < 8; ++m) {
+                    const int r = t + m * T;
+                    const unsigned lo = off[r] - base, hi = off[r + 1] - base;
+                    if (hi - lo <= (unsigned)WQ_SMALL) {
+                        int re = 0, im = 0;  // exact: at most WQ_SMALL entries below 2^22
+                        for (unsigned k = lo; k < hi; ++k) {
+                            const unsigned u = items[k];
+                            const int idx = ((int)(u & 0xfffu) * col) & kmask;
+                            const int2 w = wq[idx + (idx >> 4)];
+                            const bool odd = (u >> 31) != 0;  // the odd slice of the pair: i W^m
+                            re += odd ? -w.y : w.x;
+                            im += odd ? w.x : w.y;
+                        }
+                        v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
+                    } else {
+                        long long re = 0, im = 0;
+                        for (unsigned k = lo; k < hi; ++k) {
+                            const unsigned u = items[k];
+                            const int idx = ((int)(u & 0xfffu) * col) & kmask;
+                            const int2 w = wq[idx + (idx >> 4)];
+                            const bool odd = (u >> 31) != 0;
+                            re += odd ? -w.y : w.x;
+                            im += odd ? w.x : w.y;
+                        }
+                        v[m] = make_float2((float)re * INV_SCALE, (float)im * INV_SCALE);
+                    }
+                }
+                fft::fft_regs<N, false, false>(v, sm, b, t, addr, a.tw);
+    #pragma unroll
+                for (int m = 0; m < 8; ++m) {
+                    acc[m].x = fmaf(f[m], v[m].x, acc[m].x);
+                    acc[m].y = fmaf(f[m], v[m].y, acc[m].y);
+                }
+            }
+            fft::fft_regs<N, true, false>(acc, sm, b, t, addr, a.tw);
+            float2* dst = a.work + y * npix + col;
+    #pragma unroll
+            for (int m = 0; m < 8; ++m) dst[(long long)(t + m * T) * ld] = acc[m];
+        }
+    }
+    // the tiles outside the filters' support: zero spectra
+    const int dead = tiles - live;
+    const long long n_dead = (long long)a.n_img * P * dead;
+    for (long long d = blockIdx.x; d < n_dead; d += gridDim.x) {
+        const long long y = d / dead;
+        const int img = (int)(y / P);
+        const int pair = a.pair0 + (int)(y - (long long)img * P);
+        if (a.img_slices && 2 * pair >= a.img_slices[img]) continue;
+        const int col = (lt_lo + (int)(d - y * dead)) * B + b;
+        float2* dst = a.work + y * npix + col;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) dst[(long long)(t + m * T) * ld] = make_float2(0.f, 0.f);
+    }
+}
+
 // From length 512 the same pass runs as persistent CTAs of 512 threads with 16 values per
 // thread (the radix-16 column transforms of the wave passes, twiddles staged in shared
 // memory up to 2048).  They take runs of `run` consecutive live column tiles, in (image,
@@ -373,36 +518,73 @@ __global__ void __launch_bounds__(512, 1) slice_cols_atoms16_kernel(SliceArgs a,
     }
 }
 
+// Tiles per work-queue run: up to 16 of one pair (a handful of queue operations per
+// pair), fewer when that would leave fewer than 8 runs per CTA (the tail).
+inline int queue_run(int live, long long planes, int grid) {
+    long long run = live < 16 ? (live > 0 ? live : 1) : 16;
+    const long long n_live = planes * live;
+    while (run > 1 && n_live < run * 8LL * grid) run >>= 1;
+    return (int)run;
+}
+
 template <int N>
 int slice_cols_atoms_n(const SliceArgs& a, cudaStream_t st) {
     constexpr int T = N / 8;
     const int B = col_B_for(N, a.n2);
     const size_t off_bytes = (size_t)a.n_elems * (N + 1) * sizeof(unsigned);
-    // persistent with 16 values per thread from length 512 (1.15x the per-tile form at
-    // 2048^2 and on 512^2 blobs); the per-tile form below 512, where its many small CTAs
-    // already overlap their staging
-    if constexpr (N >= 512) {
-        using C = ColAtoms16<N>;
-        if (off_bytes <= (size_t)OFF_CACHE_BYTES && a.tile_counter != nullptr && a.n2 >= C::B) {
-            const int tiles = a.n2 / C::B;
-            int lt_lo = (a.live_lo + C::B - 1) / C::B, lt_hi = (a.live_hi + C::B - 1) / C::B;
+    // Persistent from length 512, on the work queue.  From 2048 (tiles of at most 4
+    // columns) with 16 values per thread and per-atom sums: 1.15x the per-tile form on the
+    // 2048^2 slab (about 4,200 atoms per slice pair).  Per-atom sums cost each atom B table
+    // lookups and 2B shared-memory atomics, and they lose to the per-row sums in registers
+    // on wide tiles and on dense planes (a 512^2 group of iced blobs, 16 columns per tile
+    // and ~26k atoms per slice pair, ran 3.5x slower that way): there, and at 512 and 1024,
+    // the 8-value form with per-row sums runs (1.11x the per-tile form on 512^2 blobs).
+    // Below 512 the per-tile form, whose many small CTAs already overlap their staging.
+    if (off_bytes <= (size_t)OFF_CACHE_BYTES && a.tile_counter != nullptr) {
+        const long long planes = (long long)a.n_img * a.n_pairs;
+        const long long per_plane = planes > 0 ? (long long)a.n_atoms / planes : 0;
+        if constexpr (N >= 2048) {
+            using C = ColAtoms16<N>;
+            if (a.n2 >= C::B && per_plane <= ITEM_CACHE) {
+                const int tiles = a.n2 / C::B;
+                int lt_lo = (a.live_lo + C::B - 1) / C::B, lt_hi = (a.live_hi + C::B - 1) / C::B;
+                if (a.live_lo < 0 || a.live_hi < 0) lt_lo = lt_hi = 0;
+                if (lt_lo + lt_hi >= tiles) {
+                    lt_lo = tiles;
+                    lt_hi = 0;
+                }
+                const size_t smem = ((size_t)C::B * C::STRIDE + C::TW) * sizeof(float2) +
+                                    (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) + off_bytes +
+                                    a.n_elems * sizeof(int) + (size_t)ITEM_CACHE * sizeof(unsigned);
+                const void* k = (const void*)slice_cols_atoms16_kernel<N>;
+                EMSIM_TRY(ensure_smem_attr(k, smem));
+                const long long n_tiles = (long long)a.n_img * a.pairs_here() * tiles;
+                const int grid = persistent_grid(k, 512, smem, (int)(n_tiles < (1 << 30) ? n_tiles : (1 << 30)));
+                const int run = queue_run(lt_lo + lt_hi, (long long)a.n_img * a.pairs_here(), grid);
+                EMSIM_CHECK_CUDA(cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned), st));
+                slice_cols_atoms16_kernel<N><<<grid, 512, smem, st>>>(a, lt_lo, lt_hi, run);
+                EMSIM_CHECK_LAUNCH();
+                return EMSIM_GB300_OK;
+            }
+        }
+        if constexpr (N >= 512) {
+            const int tiles = a.n2 / B;
+            int lt_lo = (a.live_lo + B - 1) / B, lt_hi = (a.live_hi + B - 1) / B;
             if (a.live_lo < 0 || a.live_hi < 0) lt_lo = lt_hi = 0;
             if (lt_lo + lt_hi >= tiles) {
                 lt_lo = tiles;
                 lt_hi = 0;
             }
-            const size_t smem = ((size_t)C::B * C::STRIDE + C::TW) * sizeof(float2) +
-                                (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) + off_bytes + a.n_elems * sizeof(int) +
+            const size_t smem = (size_t)(N + N / 8) * B * sizeof(float2) +
+                                (size_t)(a.n2 + a.n2 / 16 + 1) * sizeof(int2) + off_bytes +
                                 (size_t)ITEM_CACHE * sizeof(unsigned);
-            const void* k = (const void*)slice_cols_atoms16_kernel<N>;
+            const void* k = (const void*)slice_cols_atoms_persist_kernel<N>;
             EMSIM_TRY(ensure_smem_attr(k, smem));
             const long long n_tiles = (long long)a.n_img * a.pairs_here() * tiles;
-            const int grid = persistent_grid(k, 512, smem, (int)(n_tiles < (1 << 30) ? n_tiles : (1 << 30)));
-            // runs of up to 16 tiles of one pair: a handful of queue operations per pair
-            const int live = lt_lo + lt_hi;
-            const int run = live < 16 ? (live > 0 ? live : 1) : 16;
+            const int grid = persistent_grid(k, B * T, smem, (int)(n_tiles < (1 << 30) ? n_tiles : (1 << 30)));
+            const int run = queue_run(lt_lo + lt_hi, (long long)a.n_img * a.pairs_here(), grid);
             EMSIM_CHECK_CUDA(cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned), st));
-            slice_cols_atoms16_kernel<N><<<grid, 512, smem, st>>>(a, lt_lo, lt_hi, run);
+            slice_cols_atoms_persist_kernel<N><<<grid, B * T, smem, st>>>(a, lt_lo, lt_hi, run);
             EMSIM_CHECK_LAUNCH();
             return EMSIM_GB300_OK;
         }

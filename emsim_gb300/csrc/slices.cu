@@ -297,6 +297,7 @@ int bucket_atoms_z(emsim_gb300_slice_plan* p, const float* coords, const int32_t
     a.bucket_off = U(w.off);
     a.items = U(w.items);
     a.tile_counter = U(w.tile_counter);
+    a.n_atoms = n_atoms;
     a.wq = p->wq;
     a.live_lo = p->col_cut + 1;
     a.live_hi = p->col_cut > 0 ? p->col_cut : 0;
@@ -481,6 +482,7 @@ int emsim_gb300_build_slices(emsim_gb300_slice_plan* p, const float* coords, uns
     a.bucket_off = U(w.off);
     a.items = U(w.items);
     a.tile_counter = U(w.tile_counter);
+    a.n_atoms = n_atoms;
     a.wq = p->wq;
     a.live_lo = p->col_cut + 1;
     a.live_hi = p->col_cut > 0 ? p->col_cut : 0;

@@ -19,6 +19,7 @@ struct SliceArgs {
     const int2* wq = nullptr;              // W_n2^m then i W_n2^m, m < n2, WQ_SCALE fixed point
     const int* img_slices = nullptr;       // per image slice count (<= n_slices); pairs beyond are skipped
     unsigned* tile_counter = nullptr;      // one word of device scratch: the column pass's work queue
+    unsigned n_atoms = 0;                  // atoms bucketed (all images and elements): sizes the planes
     // columns [0, live_lo) and [n2 - live_hi, n2) hold the filters' support (T_e nonzero
     // for some element and row); every other column of the slice spectra is zero
     int live_lo = 0, live_hi = 0;
