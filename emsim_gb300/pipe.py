@@ -348,6 +348,9 @@ class Pipe:
         dev = backend._device()
         b = bufs.get(buf_key)
         if b is None or b["xyz"].device != dev or b["xyz"].shape[0] < n_atoms or b["shift"].shape[0] < nm:
+            if b is not None and b["busy"] is not None:
+                # the old buffers and the graphs that read them go: their last batch must be done
+                b["busy"].synchronize()
             cap = max(n_atoms, 1024 if b is None else b["xyz"].shape[0])
             capm = max(nm, 16 if b is None else b["shift"].shape[0])
             b = {"xyz": torch.empty((cap, 3), dtype=torch.float32, device=dev),
@@ -504,6 +507,8 @@ class Pipe:
             cap = self._chunk_stream((buf_key, "capture"))
             cap.wait_stream(main)
             g = torch.cuda.CUDAGraph()
+            # entering the capture synchronises the device, so the graph that put() may drop
+            # below (least recently used) has no replay in flight
             with torch.cuda.graph(g, stream=cap):
                 for _, _, w in work:
                     for step in w:
