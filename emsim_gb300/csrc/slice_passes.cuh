@@ -679,8 +679,53 @@ __global__ void __launch_bounds__(256) slice_rows_inv16_kernel(SliceArgs a) {
     }
 }
 
+// lengths 1024..4096: the same pass with 16 values per thread (fft16n: radix-16 passes,
+// then one radix-2/4/8 pass), L / 16 threads per row, 256 threads per CTA, each row's
+// threads synchronising with a named barrier of their own
+template <int L>
+__global__ void __launch_bounds__(256) slice_rows_inv16n_kernel(SliceArgs a) {
+    constexpr int T = L / 16;
+    constexpr int SYNC = T <= 32 ? fft16::SYNC_WARP : fft16::SYNC_SEQ;
+    extern __shared__ float2 sm[];
+    const int b = threadIdx.x / T;
+    const int t = threadIdx.x - b * T;
+    const int B = blockDim.x / T;
+    const int row = blockIdx.x * B + b;
+    const int y = blockIdx.y;  // img * pairs_here + pair - pair0
+    const int img = y / a.pairs_here();
+    const int local = y - img * a.pairs_here();
+    const int pair = a.pair0 + local;
+    if (a.img_slices && 2 * pair >= a.img_slices[img]) return;  // past this image's stack
+    const long long npix = (long long)a.n1 * L;
+    const float2* src = a.work + (long long)y * npix + (long long)row * L;
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = src[t + m * T];
+    fft16::fft16n<L, true, SYNC>(v, sm, b, t, fft16::RowSlotN<L>{}, a.tw);
+    float* out = a.out + (long long)img * a.out_stride_slices() * npix;
+    float* o0 = out + (long long)(2 * local) * npix + (long long)row * L;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) o0[t + m * T] = clip_low(v[m].x);
+    if (2 * pair + 1 < a.n_slices) {
+        float* o1 = out + (long long)(2 * local + 1) * npix + (long long)row * L;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) o1[t + m * T] = clip_low(v[m].y);
+    }
+}
+
 template <int N>
 int slice_rows_inv_n(const SliceArgs& a, cudaStream_t st) {
+    // 16 values per thread from length 1024 (the 2048^2 slab's build 1.045x; 0.99x at 512)
+    if constexpr (N >= 1024) {
+        constexpr int B = 256 / (N / 16);  // rows per CTA
+        if (a.n1 % B == 0) {
+            const size_t smem = (size_t)B * N * sizeof(float2);
+            EMSIM_TRY(ensure_smem_attr((const void*)slice_rows_inv16n_kernel<N>, smem));
+            slice_rows_inv16n_kernel<N><<<dim3(a.n1 / B, a.n_img * a.pairs_here()), 256, smem, st>>>(a);
+            EMSIM_CHECK_LAUNCH();
+            return EMSIM_GB300_OK;
+        }
+    }
     if (N == 256 && a.n1 % 16 == 0) {
         const int B = 16;  // rows per CTA, 256 threads
         const size_t smem = (size_t)B * N * sizeof(float2);
