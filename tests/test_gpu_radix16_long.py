@@ -102,16 +102,18 @@ def test_image_lens_space_2048(eng):
     assert om.rel_l2(space, o64.space_propagate(w, 0.5)) < TOL
 
 
-@pytest.mark.parametrize("n,zs", [(512, [6, 7, 8, 16]), (2048, [6])])
-def test_slice_build_columns(eng, n, zs):
+@pytest.mark.parametrize("n,zs,n_atoms", [(512, [6, 7, 8, 16], 4000), (1024, [6, 8], 12000), (2048, [6], 30000),
+                                          (2048, [6, 8], 9000), (4096, [6], 12000)])
+def test_slice_build_columns(eng, n, zs, n_atoms):
     """The slice build with the zero column tiles outside the filters' support (at pixel
     0.1 A the scattering factors end at |k| = 4 / A, inside Nyquist), against the FP64
     oracle, with the wave passes' tuning at either value (the build keeps its own
-    column kernel)."""
+    column kernel).  The persistent column pass takes its 8-value form with per-row sums
+    at 512 and 1024 and for planes above 6,144 atoms per slice pair (2048, 30,000 atoms
+    in 3 pairs), its 16-value form with per-atom sums from 2048 otherwise."""
     autotune, backend = eng
     rng = np.random.default_rng(n + len(zs))
     d, dz, ns = 0.1, 0.5, 5
-    n_atoms = 4000 if n == 512 else 30000
     xyz = ((rng.random((n_atoms, 3)) - 0.5) * np.array([ns * dz, n * d, n * d])).astype(np.float32)
     el = rng.choice(np.array(zs), size=n_atoms)
     order = np.argsort(el, kind="stable")
