@@ -4,7 +4,7 @@ Headline workload: the amorphous-carbon slab, 838,861 C atoms uniform at 0.1 A^-
 204.8 x 204.8 x 200 A (seeded), imaged on a 2048 x 2048 wave at pixel 0.1 A through 400
 slices of 0.5 A, 300 keV, Cs 1.0 mm, Scherzer defocus and aperture, plain FP32: atom
 binning -> projected-potential slices -> multislice -> lens -> |psi|^2.  One step images
-four such slabs (four seeds, --batch).  ``value`` times that step with its atoms
+eight such slabs (eight seeds, --batch).  ``value`` times that step with its atoms
 resident in HBM (L2 flushed by a 256 MiB write before every step, CUDA events on the
 launching stream); ``e2e`` runs the same images through the public ``Pipe.submit_batch``
 API from host atoms to host images, every step copying the atoms in and the images out.
@@ -902,7 +902,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--batch", type=int, default=4, help="slab images per step (seeds rank*1000 + 0..batch-1)")
+    ap.add_argument("--batch", type=int, default=8, help="slab images per step (seeds rank*1000 + 0..batch-1)")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
