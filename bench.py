@@ -728,8 +728,9 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": round(1e3 * t_total / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (complex64 waves)", "data": "synthetic (seeded slab)",
         "config": dict(CONFIG),
-        "setup": {"images_per_step_per_gpu": step_images, "l2": "flushed (256 MiB write) before every timed step; the "
-                                                     "6.7 GB slice stack is larger than L2 too",
+        "setup": {"images_per_step_per_gpu": step_images,
+                  "l2": "flushed (256 MiB write) before every timed step; the %.1f GB of slice stacks are larger "
+                        "than L2 too" % (step_images * 4.0 * SLAB["n_slices"] * SLAB["n"] ** 2 / 1e9),
                   "cuda_graph": graph is not None, "parallelism": f"image-parallel x{world}",
                   "autotune": {k: {"row": v["row"], "col": v["col"]} for k, v in tuned.items()}},
         "slice_steps_per_s": round(value * SLAB["n_slices"], 1),
