@@ -40,7 +40,15 @@ def get_tuning(n: int) -> Dict[str, int]:
             "default_row_rows": v[5], "default_col_cols_tma": v[6], "default_col_cols": v[7]}
 
 
-def set_tuning(n: int, row_tma: int = -1, row_rows: int = 0, col_tma: int = -1, col_cols: int = 0) -> None:
+def set_tuning(n: int, row_tma: Optional[int] = None, row_rows: int = 0, col_tma: Optional[int] = None,
+               col_cols: int = 0) -> None:
+    """Set the pass kernels of length n; with neither kernel given, restore the built-in
+    setting (the 16-value kernels at 256, 1024, 2048 and 4096, TMA radix-8 elsewhere)."""
+    if row_tma is None and col_tma is None:
+        _native.call("emsim_gb300_set_pass_tuning", int(n), -2, 0, -1, 0)
+        return
+    row_tma = -1 if row_tma is None else row_tma
+    col_tma = -1 if col_tma is None else col_tma
     _native.call("emsim_gb300_set_pass_tuning", int(n), int(row_tma), int(row_rows), int(col_tma), int(col_cols))
 
 

@@ -187,20 +187,44 @@ EMSIM_FAST_SIZES(EMSIM_DECL)
 #undef EMSIM_DECL
 
 
-// tuning table indexed by log2(n), n = 8 .. 4096
-PassTuning g_tuning[13];
-std::mutex g_tuning_mu;
-
 static int log2_fast(int n) {
     int k = 0;
     while ((1 << k) < n) ++k;
     return k;
 }
 
+// Built-in setting per length, as measured fastest on GB300 (µs per multislice step,
+// TMA radix-8 against 16 values per thread): 256^2 x 16 images 18.9 / 15.2 (4 rows, 8
+// columns per tile); 1024^2 x 8 96.8 / 84.6; 2048^2 x 1 63.5 / 54.7 (1 row per tile);
+// 4096^2 x 1 277 / 207; at 512^2 the TMA radix-8 kernels win (19.6 / 20.6 x 4 images).
+static PassTuning default_tuning(int n) {
+    PassTuning t;
+    switch (n) {
+        case 256: t = {2, 4, 2, 8}; break;
+        case 1024: t = {2, 0, 2, 0}; break;
+        case 2048: t = {2, 1, 2, 0}; break;
+        case 4096: t = {2, 0, 2, 0}; break;
+        default: break;
+    }
+    return t;
+}
+
+// tuning table indexed by log2(n), n = 8 .. 4096
+static PassTuning* tuning_table() {
+    static PassTuning table[13];
+    static bool init = [] {
+        for (int k = 3; k <= 12; ++k) table[k] = default_tuning(1 << k);
+        return true;
+    }();
+    (void)init;
+    return table;
+}
+std::mutex g_tuning_mu;
+
 PassTuning pass_tuning(int n) {
     if (!fast_len(n)) return PassTuning{};
     std::lock_guard<std::mutex> lk(g_tuning_mu);
-    return g_tuning[log2_fast(n)];
+    return tuning_table()[log2_fast(n)];
 }
 
 int launch_row(int n2, int ops, const RowArgs& a, int n_img, cudaStream_t st) {
@@ -545,12 +569,17 @@ extern "C" int emsim_gb300_abi_version(void) { return EMSIM_GB300_ABI_VERSION; }
 extern "C" int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int col_tma, int col_cols) {
     using namespace emsim_gb300;
     EMSIM_REQUIRE(fast_len(n), EMSIM_GB300_ERR_INVALID, "set_pass_tuning: n must be a power of two in [8, 4096]");
+    if (row_tma == -2) {  // the built-in setting
+        std::lock_guard<std::mutex> lk(g_tuning_mu);
+        tuning_table()[log2_fast(n)] = default_tuning(n);
+        return EMSIM_GB300_OK;
+    }
     EMSIM_REQUIRE(row_tma >= -1 && row_tma <= 2 && col_tma >= -1 && col_tma <= 2 && row_rows >= 0 && col_cols >= 0,
                   EMSIM_GB300_ERR_INVALID,
                   "set_pass_tuning: row and column kernels in {-1, 0, 1, 2 (16 values per thread, lengths 256..4096)}, "
-                  "tiles >= 0");
+                  "tiles >= 0 (row_tma -2: the built-in setting)");
     std::lock_guard<std::mutex> lk(g_tuning_mu);
-    PassTuning& t = g_tuning[log2_fast(n)];
+    PassTuning& t = tuning_table()[log2_fast(n)];
     t.row_tma = row_tma == 1 ? -1 : row_tma;
     t.row_rows = row_rows;
     t.col_tma = col_tma == 1 ? -1 : col_tma;

@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(512, 1)
 template <int L>
 bool launch_row16_n(int ops, const RowArgs& a, int n_img, cudaStream_t st, int* status) {
     using C = r16::RowCfg<L>;
-    if (pass_tuning(L).row_tma != 2 || (ops & (ROW_STORE_PHI | ROW_GRAD))) return false;
+    if (pass_tuning(L).row_tma != 2 || !tma_enabled() || (ops & (ROW_STORE_PHI | ROW_GRAD))) return false;
     if (!(ops & ROW_CONST_IN) && !aligned16(a.in)) return false;
     if ((ops & ROW_TRANSMIT) && (!aligned16(a.slice) || (a.slice_img_stride & 3) != 0)) return false;
     int B = tile_with_hint(C::THREADS / C::T, pass_tuning(L).row_rows, 1);
@@ -330,7 +330,7 @@ bool launch_row16_n(int ops, const RowArgs& a, int n_img, cudaStream_t st, int* 
 template <int L>
 bool launch_col16_n(int mode, const ColArgs& a, int n_img, cudaStream_t st, int* status) {
     using C = r16::ColCfg<L>;
-    if (pass_tuning(L).col_tma != 2 || !aligned16(a.data)) return false;
+    if (pass_tuning(L).col_tma != 2 || !tma_enabled() || !aligned16(a.data)) return false;
     int B = C::THREADS / C::T;
     if (B > a.n_cols) B = a.n_cols;
     B = tile_with_hint(B, pass_tuning(L).col_cols, 2);

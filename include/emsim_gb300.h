@@ -353,11 +353,15 @@ int emsim_gb300_multislice_image_adjoint(emsim_gb300_wave_plan* plan, const floa
 /* ---------------------------------------------------------------------------------
  * Pass tuning (no counterpart in the reference, whose FFTs are cuFFT / FFTW plans).
  * For wave passes of length n (power of two in [8, 4096]): whether the TMA-staged
- * persistent kernel may run (row_tma / col_tma: -1 or 1 = when it applies, 0 = never) and
- * the rows / columns per tile (0 = built-in; a smaller power of two is honoured).  Tiles
- * regroup independent rows or columns only, so results are identical for every setting.
- * The table is process-wide; emsim_gb300.autotune measures candidates and caches the
- * choice per GPU and size.
+ * persistent kernel may run (row_tma / col_tma: -1 or 1 = when it applies, 0 = never,
+ * 2 = the kernels with 16 values per thread, lengths 256..4096) and the rows / columns per
+ * tile (0 = built-in; a smaller power of two is honoured).  Tiles regroup independent rows
+ * or columns only, so results are identical for every setting of one kernel family.
+ * row_tma = -2 restores the built-in setting of length n (the other arguments are then
+ * ignored): the 16-value kernels at 256 (4 rows, 8 columns per tile), 1024, 2048 (1 row
+ * per tile) and 4096, the TMA kernels elsewhere, as measured fastest on GB300.  The table
+ * is process-wide; emsim_gb300.autotune measures candidates and caches the choice per GPU
+ * and size.
  * ------------------------------------------------------------------------------- */
 int emsim_gb300_set_pass_tuning(int n, int row_tma, int row_rows, int col_tma, int col_cols);
 /* out[0..3]: the current setting; out[4..7]: built-in tiles of the TMA row, simple row,

@@ -198,8 +198,12 @@ def test_pass_tuning_table_host_side():
     lib = _native.load()
     out = (ctypes.c_int * 8)()
     assert lib.emsim_gb300_get_pass_tuning(256, out) == 0
-    assert list(out)[:4] == [-1, 0, -1, 0]
+    assert list(out)[:4] == [2, 4, 2, 8]  # built-in: the 16-value kernels, 4 rows and 8 columns per tile
     assert list(out)[4:] == [8, 8, 16, 16]  # built-in tiles at 256: 256 threads / 32 per row, 512 / 32 columns
+    for n, want in [(512, [-1, 0, -1, 0]), (1024, [2, 0, 2, 0]), (2048, [2, 1, 2, 0]), (4096, [2, 0, 2, 0]),
+                    (64, [-1, 0, -1, 0])]:
+        lib.emsim_gb300_get_pass_tuning(n, out)
+        assert list(out)[:4] == want, n
     assert lib.emsim_gb300_set_pass_tuning(256, 0, 4, 1, 8) == 0
     lib.emsim_gb300_get_pass_tuning(256, out)
     assert list(out)[:4] == [0, 4, -1, 8]
@@ -210,8 +214,10 @@ def test_pass_tuning_table_host_side():
     assert lib.emsim_gb300_set_pass_tuning(256, 2, 4, -1, 0) == 0
     lib.emsim_gb300_get_pass_tuning(256, out)
     assert list(out)[:2] == [2, 4]
-    assert lib.emsim_gb300_set_pass_tuning(256, -1, 0, -1, 0) == 0
     assert lib.emsim_gb300_set_pass_tuning(256, -1, -3, -1, 0) == 1
+    assert lib.emsim_gb300_set_pass_tuning(256, -2, 0, 0, 0) == 0  # back to the built-in setting
+    lib.emsim_gb300_get_pass_tuning(256, out)
+    assert list(out)[:4] == [2, 4, 2, 8]
 
 
 def test_synthetic_blob_matches_oracle_generator():
